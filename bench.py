@@ -1,0 +1,378 @@
+#!/usr/bin/env python3
+"""LBM-PSM coupling-step throughput on GB300: D3Q19 PSM MLUPS and % of the
+HBM roofline, FP32 storage against the plain FP64 path.
+
+Workload (the sheared dense suspension): D3Q19 256^3 lattice, x and z
+periodic, Zou-He moving walls in y (top +0.01, bottom -0.01 lattice units,
+`fix lbm-psm-bc shear`), tau = 0.65, 2000 spheres of diameter 12 lattice
+units placed by seeded random sequential addition (solid fraction ~0.108),
+zero particle velocities.  Synthetic data: no dataset is involved.  One
+"step" is one LBM coupling step: particle map, fused collide + stream,
+per-particle force/torque/stresslet reduction, and the wall boundary
+condition.  The particles stay in place (their motion is the host DEM's
+job), but the map is recomputed every step exactly as for moving particles.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line on rank 0.  `value` is measured with the particle
+images resident in HBM and the step sequence replayed as a CUDA graph;
+`e2e` runs the same steps through the host-pointer C-ABI call (images copied
+up from pinned memory and forces copied back every step).  The lattice
+(1.27 GB in FP32) is ~10x larger than L2, so no L2 flush is needed between
+steps.  `--impl reference` times the CPU oracle (the reference algorithm
+restated in C, FP64, all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lammps-lbm-psm_gb300")
+sys.path.insert(0, PKG)
+
+EDGE = 256
+NSPHERES = 2000
+DIAM = 12.0
+TAU = 0.65
+U_WALL = 0.01
+SEED = 20261203
+METRIC = "D3Q19 PSM MLUPS & % HBM roofline, FP32 vs FP64 at fixed drag error, 1 GB300"
+BYTES_PER_NODE = {"fp64": 2 * 19 * 8, "fp32": 2 * 19 * 4, "fp16": 2 * 19 * 2}
+
+
+def workload_params(edge=EDGE):
+    lc = DIAM
+    nu = (TAU - 0.5) / 3.0
+    Re = U_WALL * lc / nu
+    # x, z periodic: edge nodes span edge*dx; y walls: edge nodes span (edge-1)*dx
+    return dict(dimension=3, boxlo=(0.0, 0.0, 0.0), prd=(float(edge), float(edge - 1), float(edge)),
+                periodic=(1, 0, 1), nevery=1, Nlc=int(DIAM) + 1, lc=lc, rho=1.0, nu=nu, Re=Re,
+                tau=TAU, Fext=(0.0, 0.0, 0.0))
+
+
+def rsa_spheres(edge=EDGE, n=NSPHERES, d=DIAM, seed=SEED):
+    """Seeded random sequential addition, minimum image in the periodic x, z."""
+    rng = np.random.default_rng(seed)
+    L = np.array([edge, edge - 1.0, edge])
+    r = d / 2
+    acc = np.zeros((n, 3))
+    k = 0
+    tries = 0
+    while k < n:
+        tries += 1
+        if tries > 200 * n:
+            raise RuntimeError("random sequential addition did not converge")
+        c = np.array([rng.uniform(0, L[0]), rng.uniform(r + 1.0, L[1] - r - 1.0), rng.uniform(0, L[2])])
+        if k:
+            dlt = acc[:k] - c
+            for ax in (0, 2):
+                dlt[:, ax] -= L[ax] * np.round(dlt[:, ax] / L[ax])
+            if np.min(np.einsum("ij,ij->i", dlt, dlt)) < d * d:
+                continue
+        acc[k] = c
+        k += 1
+    return acc, np.full(n, r)
+
+
+def images(edge=EDGE):
+    from lbmpsm.host import Domain, ghost_images
+    x, r = rsa_spheres(edge)
+    n = len(x)
+    prm = workload_params(edge)
+    lo = prm["boxlo"]
+    hi = tuple(a + b for a, b in zip(lo, prm["prd"]))
+    dom = Domain(3, lo, hi, prm["periodic"])
+    return ghost_images(dom, DIAM / 2 + 3.0, np.arange(1, n + 1), x, np.zeros((n, 3)), np.zeros((n, 3)), r), n
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [s.strip() for s in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic of the collide kernel at the bench size, from
+    the committed ncu summary (profiles/collide_f32_d3q19_256.md), else None."""
+    path = os.path.join(ROOT, "profiles", "collide_f32_d3q19_256.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args, rank=0, world=1):
+    import torch
+
+    import lbmpsm
+
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    g, nloc = images()
+    n = len(g.tag)
+    prm = workload_params()
+    nodes = EDGE * EDGE * EDGE
+
+    def make(storage):
+        lat = lbmpsm.Lattice(**prm, storage=storage, device=device, max_images=n,
+                             max_radius=DIAM / 2)
+        lat.set_bc("shear")
+        return lat
+
+    def ev_time(lat, fn):
+        s = torch.cuda.ExternalStream(lat.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        lat.synchronize()
+        torch.cuda.synchronize()
+        e0.record(s)
+        fn()
+        e1.record(s)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    K, W = args.steps, args.warmup
+    # FP32 storage: the headline path
+    lat = make("fp32")
+    lat.step(g.tag, g.x, g.v, g.omega, g.radius)  # images go up once, map + step
+    lat.apply_bc()
+    lat.run_fixed(W)
+    lat.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(device) as clk:
+        t_val = ev_time(lat, lambda: lat.run_fixed(K))
+    t_val = max_over_ranks(t_val, world)
+    f32_forces = lat.read_forces(nloc)[0]
+
+    # end to end: host arrays through lbmpsm_step, copies every step
+    t0 = time.perf_counter()
+    for _ in range(K):
+        lat.step(g.tag, g.x, g.v, g.omega, g.radius)
+        lat.apply_bc()
+    lat.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+
+    # the collide-stream kernel alone (lattice-only steps, particle table in place)
+    def lattice_only(lt, steps):
+        def go():
+            for _ in range(steps):
+                lt.step_device(0, None, None, None, None, None)
+        return go
+    t_kernel = ev_time(lat, lattice_only(lat, K)) / K
+    lat.close()
+
+    # plain FP64 path on the same workload
+    lat64 = make("fp64")
+    lat64.step(g.tag, g.x, g.v, g.omega, g.radius)
+    lat64.apply_bc()
+    K64 = max(3, K // 4)
+    lat64.run_fixed(max(0, W + K - K64))  # same step count as the FP32 forces above
+    lat64.synchronize()
+    t64 = ev_time(lat64, lambda: lat64.run_fixed(K64))
+    f64_forces = lat64.read_forces(nloc)[0]
+    t64_kernel = ev_time(lat64, lattice_only(lat64, 3)) / 3
+    lat64.close()
+
+    mlups = nodes * K * world / t_val / 1e6
+    mlups64 = nodes * K64 / t64 / 1e6
+    drag_err = float(np.abs(f32_forces - f64_forces).max() / np.abs(f64_forces).max())
+    peak, peak_kind = measured_peak_gbs()
+    achieved = BYTES_PER_NODE["fp32"] * nodes / t_kernel / 1e9
+    traffic = profile_traffic()
+    launches_per_step = 8  # map: prep, scan, fill, sort, apply; collide; reduce; bc
+    out = {
+        "metric": METRIC,
+        "value": round(mlups, 1),
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": round(t_val / K * 1e3, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": "sheared suspension: D3Q19 256^3, y Zou-He shear walls +-0.01, tau 0.65, "
+                        "2000 spheres D=12 (seeded RSA, phi~0.108), FP32 storage, FP64 F/T/S",
+            "nodes": nodes, "particles": nloc, "images": n, "storage": "fp32",
+            "l2": "lattice 1.27 GB > 129 MB L2: no flush needed",
+            "parallelism": f"replicas x{world}",
+        },
+        "e2e": {"value": round(nodes * K / t_e2e / 1e6, 1), "unit": "MLUPS",
+                "h2d_bytes_per_step": int(n * (4 + 10 * 8)), "d2h_bytes_per_step": int(n * 12 * 8)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "kernel": "collide_lowp_kernel<D3Q19,float> (A-A, even/odd)",
+                     "algorithmic_bytes_per_node": BYTES_PER_NODE["fp32"],
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "fp64_plain": {"value": round(mlups64, 1), "unit": "MLUPS",
+                       "kernel_ms": round(t64_kernel * 1e3, 3),
+                       "hbm_frac": round(BYTES_PER_NODE["fp64"] * nodes / t64_kernel / 1e9 / peak, 4)},
+        "fp32_over_fp64": round(mlups / world / mlups64, 2),
+        "drag_rel_err_fp32_vs_fp64": drag_err,
+        "kernel_ms": round(t_kernel * 1e3, 4),
+        "gpu_launches": launches_per_step * K,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_steps)
+    return out
+
+
+def max_over_ranks(t, world):
+    if world <= 1:
+        return t
+    import torch
+    v = torch.tensor([t], dtype=torch.float64, device="cuda")
+    torch.distributed.all_reduce(v, op=torch.distributed.ReduceOp.MAX)
+    return float(v.item())
+
+
+def cpu_baseline(steps, threads=None):
+    """The CPU oracle (FP64, the reference's layout and arithmetic) on the same
+    workload, all host cores, a bounded number of coupling steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liblbmpsm_oracle.so"], check=True)
+    threads = threads or os.cpu_count()
+    g, nloc = images()
+    prm = workload_params()
+    prm["bc_type"] = 1
+    sim = pyoracle.Sim("restatement", **prm)
+    sim.set_threads(threads)
+    sim.step(g.tag, g.x, g.v, g.omega, g.radius, bc=True)  # warm-up (first touch)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step(g.tag, g.x, g.v, g.omega, g.radius, bc=True)
+    dt = time.perf_counter() - t0
+    sim.close()
+    nodes = EDGE ** 3
+    return {"value": round(nodes * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": threads,
+            "kind": "port",
+            "sample": f"{steps} full coupling steps of the same 256^3 / 2000-sphere workload "
+                      f"(after 1 warm-up step), FP64, OpenMP over {threads} threads",
+            "seconds": round(dt, 2)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    cb = cpu_baseline(max(1, args.steps))
+    nodes = EDGE ** 3
+    return {
+        "metric": METRIC, "value": cb["value"], "unit": "MLUPS", "n_gpus": world,
+        "steps": max(1, args.steps), "warmup": 1,
+        "ms_per_step": round(cb["seconds"] / max(1, args.steps) * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": "sheared suspension: D3Q19 256^3, y Zou-He shear walls +-0.01, "
+                               "tau 0.65, 2000 spheres D=12 (seeded RSA, phi~0.108)",
+                   "nodes": nodes, "parallelism": f"{cb['cores']} host threads"},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * lbmpsm.h -- C ABI of the GB300 lattice-Boltzmann partially-saturated-cell
+ * (PSM) library (liblbmpsm_gb300.so).
+ *
+ * The library replaces the LBM library behind the LAMMPS commands
+ * `fix lbm-psm`, `fix lbm-psm-bc` and `fix lbm-psm-vti` of
+ * timnajuch/LAMMPS-LBM-PSM.  The LAMMPS host keeps time integration,
+ * neighbour lists, ghost atoms, reverse communication and the lubrication
+ * pair style; each entry point below replaces one call site of the reference
+ * (cited per function, paths relative to the reference repository).
+ *
+ * Conventions
+ *   - Plain C types only; arrays of 3-vectors are row-major n x 3 (the
+ *     layout of LAMMPS' contiguous double** atom arrays, pass x[0]).
+ *   - Every function returns LBMPSM_OK (0) or a negative LBMPSM_ERR_* code;
+ *     lbmpsm_last_error() gives the message.  Where the reference calls
+ *     error->all() the library returns an error instead; nothing exits or
+ *     throws across the ABI.
+ *   - One handle = one lattice resident on one GPU, one CUDA stream.  Calls
+ *     on a handle must come from one thread at a time.  Host-pointer calls
+ *     are synchronous; *_device calls are asynchronous on the handle's stream.
+ *   - Node layouts exchanged with the host follow the reference lattice
+ *     (src/LBM_PSM_lattice.h:88-90): node (i*ny + j)*nz + k over the local
+ *     array including the one-node halo, populations f[node*q + iq].
+ */
+#ifndef LBMPSM_H
+#define LBMPSM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBMPSM_ABI_VERSION 1
+
+/* status codes */
+#define LBMPSM_OK 0
+#define LBMPSM_ERR_ARG (-1)      /* "Illegal fix lbm-psm command" and bad arguments */
+#define LBMPSM_ERR_MACH (-2)     /* Ma > 0.3 (src/fix_LBM_PSM.cpp:122-125) */
+#define LBMPSM_ERR_GRID (-3)     /* domain / dx not integral (src/fix_LBM_PSM.cpp:135-140) */
+#define LBMPSM_ERR_NOMEM (-4)    /* device or pinned host allocation failed */
+#define LBMPSM_ERR_CUDA (-5)     /* a CUDA runtime call failed */
+#define LBMPSM_ERR_STATE (-6)    /* call not valid in the handle's current state */
+#define LBMPSM_ERR_CAPACITY (-7) /* more particle images than the handle was sized for */
+#define LBMPSM_ERR_NUMERIC (-8)  /* non-finite populations or mass drift detected */
+#define LBMPSM_ERR_TIMEOUT (-9)  /* a bounded device-side wait gave up */
+
+/* population storage of the lattice */
+#define LBMPSM_STORAGE_FP64 0 /* plain FP64, the reference arithmetic */
+#define LBMPSM_STORAGE_FP32 1 /* FP32 deviations f_i - w_i*rho0, FP32 collision */
+#define LBMPSM_STORAGE_FP16 2 /* FP16 scaled deviations, FP32 collision */
+
+/* `fix lbm-psm-bc` keywords (src/fix_LBM_PSM_BC.cpp:21-39) */
+#define LBMPSM_BC_NONE 0
+#define LBMPSM_BC_SHEAR 1
+#define LBMPSM_BC_XFLOW 2
+#define LBMPSM_BC_CHANNEL 3
+#define LBMPSM_BC_CHANNEL_VELIN_PRESSOUT 4
+#define LBMPSM_BC_CLOSEDBOX 5
+
+/* PSM weighting B_n of the solid operator */
+#define LBMPSM_WEIGHT_REFERENCE 0 /* B_n = eps_n, renormalised when sum > 1 (reference) */
+#define LBMPSM_WEIGHT_NOBLE_TORCZYNSKI 1 /* B_n = eps_n(tau-1/2)/((1-eps_n)+(tau-1/2)) */
+
+typedef struct lbmpsm_handle lbmpsm_handle;
+
+/* Arguments of `fix lbm-psm` (src/fix_LBM_PSM.cpp:15-83) plus the LAMMPS
+ * domain that fix_LBM_PSM::init() reads (src/fix_LBM_PSM.cpp:104-177). */
+typedef struct {
+  int dimension;   /* domain->dimension: 2 or 3 */
+  double boxlo[3]; /* domain->boxlo */
+  double prd[3];   /* domain->xprd, yprd, zprd */
+  int periodic[3]; /* domain->xperiodic, yperiodic, zperiodic */
+  int nevery;      /* every */
+  int Nlc;         /* Nlc */
+  double lc, rho, nu, Re;
+  double tau;      /* tau (the fix's default is 0.7) */
+  double Fext[3];  /* Fext fx fy fz (physical volume force) */
+} lbmpsm_fix_params;
+
+/* Options that have no counterpart in the reference (defaults: all zero). */
+typedef struct {
+  int storage;       /* LBMPSM_STORAGE_* */
+  int device;        /* CUDA device ordinal */
+  int max_images;    /* particle images per step the handle is sized for (0: 4096, grows
+                        on host-pointer calls) */
+  double max_radius; /* largest particle radius, physical units (0: derived per call on
+                        host-pointer calls; required for *_device calls) */
+  int psm_weighting; /* LBMPSM_WEIGHT_* */
+} lbmpsm_options;
+
+/* Derived quantities of fix_LBM_PSM::init and UnitConversion
+ * (src/LBM_PSM_unitConversion.cpp:15-38). */
+typedef struct {
+  int dimension, q;
+  int nx, ny, nz;        /* global node counts as fix init computes them (nz = 0 in 2-D) */
+  int local[3];          /* reference local array incl. halo: nx+2, ny+2, nz+2 (1 in 2-D) */
+  int storage_dims[3];   /* device array extents (periodic axes carry no halo) */
+  double dx, Uc, u_lb, tc, dt_d;
+  double forceFactor, torqueFactor, volumeForceFactor;
+  double dt_dem;         /* the DEM timestep fix init writes to update->dt */
+  double Ma;
+  double F_lbm[3];       /* lattice-unit body force */
+  int64_t steps;         /* LBM steps done on this handle */
+  size_t device_bytes;   /* device memory held by the handle */
+} lbmpsm_info;
+
+/* Replaces fix_LBM_PSM::init (src/fix_LBM_PSM.cpp:104-177): unit conversion,
+ * Mach and grid checks, lattice allocation and initialisation to
+ * equilibrium at rho = 1, u = 0.  opts may be NULL. */
+int lbmpsm_create(const lbmpsm_fix_params* params, const lbmpsm_options* opts,
+                  lbmpsm_handle** out);
+/* Replaces ~fix_LBM_PSM (src/fix_LBM_PSM.cpp:86-93). */
+void lbmpsm_destroy(lbmpsm_handle* h);
+/* Text of the last error on this handle (or of the last failed create when
+ * h is NULL).  Never NULL. */
+const char* lbmpsm_last_error(const lbmpsm_handle* h);
+int lbmpsm_get_info(const lbmpsm_handle* h, lbmpsm_info* info);
+
+/* Replaces the keyword parsing of fix_LBM_PSM_BC (src/fix_LBM_PSM_BC.cpp:16-39)
+ * and fix_LBM_PSM_BC::init (:145-148). */
+int lbmpsm_set_bc(lbmpsm_handle* h, int bc_type);
+
+/* One LBM coupling step for n particle images (locals then ghosts, LAMMPS
+ * order), replacing the LBM branch of fix_LBM_PSM::post_force
+ * (src/fix_LBM_PSM.cpp:197-229): setParticlesOnLattice
+ * (src/LBM_PSM_exchangeParticleData.cpp:24-112), the halo exchange
+ * (src/LBM_PSM_MPICOMM.h:79-147), macroCollideStream
+ * (src/LBM_PSM_BGK_dynamics.cpp:81-109) and calculateHydrodynamicInteractions
+ * per image (src/LBM_PSM_exchangeParticleData.cpp:172-244).
+ * Inputs: tag[n], x/v/omega[n*3], radius[n] (physical units, host memory).
+ * Outputs per image, physical units, before ghost bookkeeping: fh[n*3],
+ * th[n*3], stresslet[n*6].  The caller applies f += fh (locals), f = fh
+ * (ghosts), v_tally and reverse_comm exactly as the reference fix does. */
+int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
+                const double* omega, const double* radius, double* fh, double* th,
+                double* stresslet);
+/* Same, with all arrays in device memory; asynchronous on the handle's
+ * stream.  Requires opts.max_radius >= every radius. */
+int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
+                       const double* v, const double* omega, const double* radius, double* fh,
+                       double* th, double* stresslet);
+/* Zou-He boundaries of the selected `fix lbm-psm-bc` keyword on the
+ * post-stream populations: replaces fix_LBM_PSM_BC::post_force
+ * (src/fix_LBM_PSM_BC.cpp:151-402) and ZouHeBC (src/LBM_PSM_zou_he_BC.cpp:25-398).
+ * Asynchronous on the handle's stream. */
+int lbmpsm_apply_bc(lbmpsm_handle* h);
+
+/* Macro fields.  The reference keeps rho and u arrays that macroCollideStream
+ * refreshes every step (src/LBM_PSM_BGK_dynamics.cpp:48-77); here they are
+ * written only by steps that follow a request, so that ordinary steps move
+ * only populations.  WriteVTI::pre_force reads them one step later, so the
+ * `fix lbm-psm-vti` caller requests them one LBM step before each write. */
+int lbmpsm_request_macro(lbmpsm_handle* h);
+/* Replaces the field read of WriteVTI::execute_write_vti
+ * (src/fix_LBM_PSM_writeVTI.h:146-169): interior nodes, z outermost, x
+ * innermost; solid = min(eps1+eps2, 1)*B0, rho*rho0, u*u0 (u_z = 0 in 2-D).
+ * as_double selects double (1) or float (0) output arrays; any pointer may
+ * be NULL.  Before the first requested step rho = 1 and u = 0, as after
+ * initialise_dynamics. */
+int lbmpsm_export_fields(lbmpsm_handle* h, int as_double, double B0, double rho0, double u0,
+                         void* solid, void* rho, void* u);
+
+/* Post-stream populations in the reference layout (local array with halo,
+ * f[node*q+iq], FP64).  Replaces LBMPSMLattice::getVector_f_curr /
+ * setVector_f_curr (src/LBM_PSM_lattice.cpp:230-232) as used by
+ * `fix lbm-psm-restart` (src/fix_LBM_PSM_writeReadRestart.cpp:62,75).
+ * Halo planes of periodic axes are returned as copies of the periodic twin
+ * and ignored on input. */
+int lbmpsm_get_populations(lbmpsm_handle* h, double* f);
+int lbmpsm_set_populations(lbmpsm_handle* h, const double* f);
+/* Particle table per node in the reference layout: ids[2N], eps[2N],
+ * us[6N] (LBMPSMLattice::getParticleDataOnLatticeNode,
+ * src/LBM_PSM_lattice.cpp:255).  Halo nodes of periodic axes read as empty. */
+int lbmpsm_get_particle_table(lbmpsm_handle* h, int* ids, double* eps, double* us);
+
+/* Global FP64 check (no reference counterpart): total mass and momentum of
+ * the stored nodes, and a status word that is non-zero if any population is
+ * not finite.  Returns LBMPSM_ERR_NUMERIC in that case. */
+int lbmpsm_check(lbmpsm_handle* h, double* mass, double* momentum3);
+
+/* Block until all work queued on the handle's stream is done. */
+int lbmpsm_synchronize(lbmpsm_handle* h);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their
+ * own device work after *_device calls. */
+void* lbmpsm_stream(lbmpsm_handle* h);
+
+/* Run nsteps coupling steps with the particle images already on the device
+ * (as last passed to lbmpsm_step or lbmpsm_step_device), fixed in place,
+ * each step followed by the boundary condition when one is set.  The step
+ * sequence is captured once into a CUDA graph and replayed.  Forces of the
+ * last step land in the device buffers of the last step_device call (or in
+ * the handle's own buffers after a host step; read with lbmpsm_read_forces). */
+int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps);
+/* Copy the per-image outputs of the last step to host memory. */
+int lbmpsm_read_forces(lbmpsm_handle* h, int n, double* fh, double* th, double* stresslet);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

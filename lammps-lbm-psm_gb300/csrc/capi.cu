@@ -1,0 +1,870 @@
+// capi.cu -- the extern "C" boundary of liblbmpsm_gb300.so (include/lbmpsm.h).
+//
+// A handle owns one lattice resident in HBM plus the particle-image buffers,
+// a CUDA stream and pinned staging buffers.  Host-pointer calls stage their
+// arrays through pinned memory with one copy each way per coupling step;
+// *_device calls take device arrays and stay asynchronous.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lbmpsm.h"
+#include "lbmpsm_internal.cuh"
+
+using namespace lbmpsm;
+
+struct lbmpsm_handle {
+  lbmpsm_fix_params prm{};
+  lbmpsm_options opt{};
+  Geom g{};
+  double origin[3]{};
+  // UnitConversion (src/LBM_PSM_unitConversion.cpp:15-38)
+  double nu_lb = 0, dx = 0, dx_d = 0, Uc = 0, u_lb = 0, dt_d = 0, tc = 0;
+  double forceFactor = 0, torqueFactor = 0, volumeForceFactor = 0;
+  double tau = 0, omega = 0, F_lbm[3]{};
+  double invCs2 = 0, invCs4 = 0;
+  bool has_force = false;
+  int bc_type = 0;
+  std::vector<Face> faces;
+  long long t = 0;  // LBM steps done
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  float scale16 = 4096.0f;
+  // lattice
+  void* f = nullptr;
+  Table tab{};
+  double* rho = nullptr;
+  double* u = nullptr;
+  bool macro_requested = false;
+  bool macro_valid = false;
+  // particles
+  int cap = 0;
+  long long list_cap = 0;
+  int cb[3]{8, 8, 8}, C[3]{1, 1, 1};
+  int* d_tag = nullptr;
+  double* d_xvw = nullptr;  // x | v | omega | radius, each cap entries
+  double* d_out = nullptr;  // fh | th | S  (12*cap)
+  Img* d_img = nullptr;
+  int* d_cells = nullptr;   // count | off | fill (3*ncells)
+  int* d_list = nullptr;
+  unsigned long long* d_pair_total = nullptr;
+  int* d_status = nullptr;
+  double* d_check = nullptr;
+  void* h_stage = nullptr;  // pinned: inputs then outputs
+  size_t h_stage_bytes = 0;
+  int last_n = 0;
+  // graphs of one step for each parity (map + collide + reduce + bc)
+  cudaGraphExec_t gexec[2]{nullptr, nullptr};
+  int graph_n = -1;
+  int graph_bc = -1;
+  size_t dev_bytes = 0;
+  std::string err;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+int fail(lbmpsm_handle* h, int code, const std::string& msg) {
+  if (h)
+    h->err = msg;
+  else
+    g_create_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(h, call)                                                               \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail((h), e_ == cudaErrorMemoryAllocation ? LBMPSM_ERR_NOMEM : LBMPSM_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+  } while (0)
+
+template <typename T>
+cudaError_t dmalloc(lbmpsm_handle* h, T** p, size_t bytes) {
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e == cudaSuccess) h->dev_bytes += bytes;
+  return e;
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+size_t storage_bytes(int storage) { return storage == 0 ? 8 : (storage == 1 ? 4 : 2); }
+
+// Zou-He face calls of fix_LBM_PSM_BC::post_force (src/fix_LBM_PSM_BC.cpp:223-401)
+// on one rank, converted from the reference halo frame to device storage.
+void make_faces(lbmpsm_handle* h, int bc) {
+  h->faces.clear();
+  const Geom& g = h->g;
+  const int ew = 1;
+  const int nx = g.L[0], ny = g.L[1], nz = g.L[2];
+  const double u = h->u_lb, rho_out = 1.0;
+  auto add = [&](int kind, int axis, int plane, int a0, int a1, int b0, int b1, double p0) {
+    Face fc{};
+    fc.kind = kind;
+    fc.axis = axis;
+    int lo[3], hi[3];
+    if (g.dim == 2) {
+      if (axis == 0) {
+        lo[0] = hi[0] = plane; lo[1] = a0; hi[1] = a1;
+      } else {
+        lo[1] = hi[1] = plane; lo[0] = a0; hi[0] = a1;
+      }
+      lo[2] = hi[2] = 0;
+    } else {
+      if (axis == 0) {
+        lo[0] = hi[0] = plane; lo[1] = a0; hi[1] = a1; lo[2] = b0; hi[2] = b1;
+      } else if (axis == 1) {
+        lo[1] = hi[1] = plane; lo[0] = a0; hi[0] = a1; lo[2] = b0; hi[2] = b1;
+      } else {
+        lo[2] = hi[2] = plane; lo[0] = a0; hi[0] = a1; lo[1] = b0; hi[1] = b1;
+      }
+    }
+    for (int d = 0; d < 3; ++d) {
+      fc.lo[d] = lo[d] - g.off[d];
+      fc.hi[d] = hi[d] - g.off[d];
+      fc.lo[d] = std::max(fc.lo[d], 0);
+      fc.hi[d] = std::min(fc.hi[d], g.S[d] - 1);
+    }
+    fc.plane = fc.lo[axis];
+    fc.p0 = p0;
+    if (fc.lo[0] <= fc.hi[0] && fc.lo[1] <= fc.hi[1] && fc.lo[2] <= fc.hi[2]) h->faces.push_back(fc);
+  };
+  if (g.dim == 2) {
+    switch (bc) {
+      case 1:
+        add(FACE_VEL2_YN, 1, ew, ew, nx - 1 - ew, 0, 0, -u);
+        add(FACE_VEL2_YP, 1, ny - 1 - ew, ew, nx - 1 - ew, 0, 0, u);
+        break;
+      case 2:
+        add(FACE_VEL2_XN, 0, ew, ew, ny - 1 - ew, 0, 0, u);
+        add(FACE_DENS2_XP, 0, nx - 1 - ew, ew, ny - 1 - ew, 0, 0, rho_out);
+        add(FACE_VEL2_YN, 1, ew, 1 + ew, nx - 2 - ew, 0, 0, u);
+        add(FACE_VEL2_YP, 1, ny - 1 - ew, 1 + ew, nx - 2 - ew, 0, 0, u);
+        break;
+      case 3:
+        add(FACE_VEL2_YN, 1, ew, ew, nx - 1 - ew, 0, 0, 0.0);
+        add(FACE_VEL2_YP, 1, ny - 1 - ew, ew, nx - 1 - ew, 0, 0, 0.0);
+        break;
+      case 4:
+        add(FACE_VEL2_XN, 0, ew, ew, ny - 1 - ew, 0, 0, u);
+        add(FACE_DENS2_XP, 0, nx - 1 - ew, ew, ny - 1 - ew, 0, 0, rho_out);
+        add(FACE_VEL2_YN, 1, ew, ew, nx - 1 - ew, 0, 0, 0.0);
+        add(FACE_VEL2_YP, 1, ny - 1 - ew, ew, nx - 1 - ew, 0, 0, 0.0);
+        break;
+      case 5:
+        add(FACE_VEL2_XN, 0, ew, ew, ny - 1 - ew, 0, 0, 0.0);
+        add(FACE_VEL2_XP, 0, nx - 1 - ew, ew, ny - 1 - ew, 0, 0, 0.0);
+        add(FACE_VEL2_YN, 1, ew, ew, nx - 1 - ew, 0, 0, 0.0);
+        add(FACE_VEL2_YP, 1, ny - 1 - ew, ew, nx - 1 - ew, 0, 0, 0.0);
+        break;
+      default:
+        break;
+    }
+  } else {
+    const int X0 = ew, X1 = nx - 1 - ew, Y0 = ew, Y1 = ny - 1 - ew, Z0 = ew, Z1 = nz - 1 - ew;
+    switch (bc) {
+      case 1:
+        add(FACE_VEL3_YN, 1, ew, X0, X1, Z0, Z1, -u);
+        add(FACE_VEL3_YP, 1, ny - 1 - ew, X0, X1, Z0, Z1, u);
+        break;
+      case 2:
+        add(FACE_VEL3_XN, 0, ew, Y0, Y1, Z0, Z1, u);
+        add(FACE_DENS3_XP, 0, nx - 1 - ew, Y0, Y1, Z0, Z1, rho_out);
+        add(FACE_VEL3_YN, 1, ew, X0, X1, Z0, Z1, u);
+        add(FACE_VEL3_YP, 1, ny - 1 - ew, X0, X1, Z0, Z1, u);
+        add(FACE_VEL3_ZN, 2, ew, X0, X1, Y0, Y1, u);
+        add(FACE_VEL3_ZP, 2, nz - 1 - ew, X0, X1, Y0, Y1, u);
+        break;
+      case 3:
+        add(FACE_VEL3_YN, 1, ew, X0, X1, Z0, Z1, 0.0);
+        add(FACE_VEL3_YP, 1, ny - 1 - ew, X0, X1, Z0, Z1, 0.0);
+        break;
+      case 4:
+        add(FACE_VEL3_XN, 0, ew, Y0, Y1, Z0, Z1, u);
+        add(FACE_DENS3_XP, 0, nx - 1 - ew, Y0, Y1, Z0, Z1, rho_out);
+        add(FACE_VEL3_YN, 1, ew, X0, X1, Z0, Z1, 0.0);
+        add(FACE_VEL3_YP, 1, ny - 1 - ew, X0, X1, Z0, Z1, 0.0);
+        add(FACE_VEL3_ZN, 2, ew, X0, X1, Y0, Y1, 0.0);
+        add(FACE_VEL3_ZP, 2, nz - 1 - ew, X0, X1, Y0, Y1, 0.0);
+        break;
+      case 5:
+        add(FACE_VEL3_XN, 0, ew, Y0, Y1, Z0, Z1, 0.0);
+        add(FACE_VEL3_XP, 0, nx - 1 - ew, Y0, Y1, Z0, Z1, 0.0);
+        add(FACE_VEL3_YN, 1, ew, X0, X1, Z0, Z1, 0.0);
+        add(FACE_VEL3_YP, 1, ny - 1 - ew, X0, X1, Z0, Z1, 0.0);
+        add(FACE_VEL3_ZN, 2, ew, X0, X1, Y0, Y1, 0.0);
+        add(FACE_VEL3_ZP, 2, nz - 1 - ew, X0, X1, Y0, Y1, 0.0);
+        break;
+      default:
+        break;
+    }
+  }
+}
+
+void free_particles(lbmpsm_handle* h) {
+  dfree(h->d_tag);
+  dfree(h->d_xvw);
+  dfree(h->d_out);
+  dfree(h->d_img);
+  dfree(h->d_list);
+  h->d_tag = nullptr;
+  h->d_xvw = nullptr;
+  h->d_out = nullptr;
+  h->d_img = nullptr;
+  h->d_list = nullptr;
+  if (h->h_stage) cudaFreeHost(h->h_stage);
+  h->h_stage = nullptr;
+  h->h_stage_bytes = 0;
+}
+
+void drop_graphs(lbmpsm_handle* h) {
+  for (int k = 0; k < 2; ++k)
+    if (h->gexec[k]) {
+      cudaGraphExecDestroy(h->gexec[k]);
+      h->gexec[k] = nullptr;
+    }
+  h->graph_n = -1;
+}
+
+// cells touched by one image box of width <= w nodes along each axis
+long long cells_per_image(const lbmpsm_handle* h, double r_lb) {
+  const double w = 2.0 * r_lb + 6.0;
+  long long c = 1;
+  for (int d = 0; d < 3; ++d) {
+    long long nd = (long long)std::ceil(w / h->cb[d]) + 1;
+    nd = std::min<long long>(nd, h->C[d]);
+    c *= std::max<long long>(nd, 1);
+  }
+  return c;
+}
+
+int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
+  if (n > h->cap) {
+    drop_graphs(h);
+    free_particles(h);
+    int cap = std::max(n, std::max(h->cap * 2, 1024));
+    CUDA_TRY(h, dmalloc(h, &h->d_tag, sizeof(int) * cap));
+    CUDA_TRY(h, dmalloc(h, &h->d_xvw, sizeof(double) * 10 * cap));
+    CUDA_TRY(h, dmalloc(h, &h->d_out, sizeof(double) * 12 * cap));
+    CUDA_TRY(h, dmalloc(h, &h->d_img, sizeof(Img) * cap));
+    h->h_stage_bytes = (sizeof(int) + sizeof(double) * 10 + sizeof(double) * 12) * (size_t)cap + 64;
+    CUDA_TRY(h, cudaMallocHost(&h->h_stage, h->h_stage_bytes));
+    h->cap = cap;
+    h->list_cap = 0;
+  }
+  const double r_lb = max_r_phys / h->dx;
+  const long long need = (long long)std::max(n, 1) * cells_per_image(h, r_lb);
+  if (need > h->list_cap) {
+    drop_graphs(h);
+    dfree(h->d_list);
+    h->d_list = nullptr;
+    long long cap = std::max(need, 2 * h->list_cap);
+    CUDA_TRY(h, dmalloc(h, &h->d_list, sizeof(int) * (size_t)cap));
+    h->list_cap = cap;
+  }
+  return LBMPSM_OK;
+}
+
+int collide(lbmpsm_handle* h) {
+  CollideParams p{};
+  p.g = h->g;
+  p.f = h->f;
+  p.tab = h->tab;
+  p.store_macro = h->macro_requested ? 1 : 0;
+  p.rho_out = h->rho;
+  p.u_out = h->u;
+  p.weighting = h->opt.psm_weighting;
+  p.tau = h->tau;
+  p.omega = h->omega;
+  p.one_minus_omega = 1.0 - h->omega;
+  p.guo_pref = (1.0 - 0.5 * h->omega);
+  for (int d = 0; d < 3; ++d) p.F[d] = h->F_lbm[d];
+  p.has_force = h->has_force ? 1 : 0;
+  p.invCs2 = h->invCs2;
+  p.invCs4 = h->invCs4;
+  p.scale16 = h->scale16;
+  const int odd = (int)(h->t & 1);
+  cudaError_t e;
+  switch (h->opt.storage) {
+    case LBMPSM_STORAGE_FP64: e = launch_collide_f64(p, odd, h->stream); break;
+    case LBMPSM_STORAGE_FP32: e = launch_collide_f32(p, odd, h->stream); break;
+    default: e = launch_collide_f16(p, odd, h->stream); break;
+  }
+  CUDA_TRY(h, e);
+  if (h->macro_requested) {
+    h->macro_requested = false;
+    h->macro_valid = true;
+  }
+  h->t += 1;
+  return LBMPSM_OK;
+}
+
+// map -> collide -> reduce on device image arrays (internal buffers)
+int enqueue_step(lbmpsm_handle* h, int n) {
+  // image block layout: x | v | omega (3n each) | radius (n)
+  const int* tag = h->d_tag;
+  const double* x = h->d_xvw;
+  const double* v = h->d_xvw + 3 * (size_t)n;
+  const double* w = h->d_xvw + 6 * (size_t)n;
+  const double* r = h->d_xvw + 9 * (size_t)n;
+  if (n > 0) {
+    const int ncells = h->C[0] * h->C[1] * h->C[2];
+    CUDA_TRY(h, cudaMemsetAsync(h->d_cells, 0, sizeof(int) * 3 * (size_t)ncells, h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_pair_total, 0, sizeof(unsigned long long), h->stream));
+    MapParams m{};
+    m.g = h->g;
+    m.tab = h->tab;
+    m.n = n;
+    m.tag = tag;
+    m.x = x;
+    m.v = v;
+    m.omega = w;
+    m.radius = r;
+    for (int d = 0; d < 3; ++d) m.origin[d] = h->origin[d];
+    m.dx = h->dx;
+    m.Uc = h->Uc;
+    m.u_lb = h->u_lb;
+    m.tc = h->tc;
+    m.dt_d = h->dt_d;
+    m.sqrt2half = h->g.dim == 3 ? std::sqrt(3.1) / 2.0 : std::sqrt(2.1) / 2.0;
+    m.img = h->d_img;
+    for (int d = 0; d < 3; ++d) {
+      m.cb[d] = h->cb[d];
+      m.C[d] = h->C[d];
+    }
+    m.cell_count = h->d_cells;
+    m.cell_off = h->d_cells + ncells;
+    m.cell_fill = h->d_cells + 2 * (size_t)ncells;
+    m.list = h->d_list;
+    m.list_cap = h->list_cap;
+    m.pair_total = h->d_pair_total;
+    m.status = h->d_status;
+    m.write32 = h->opt.storage != LBMPSM_STORAGE_FP64 ? 1 : 0;
+    CUDA_TRY(h, launch_map(m, h->stream));
+  }
+  int rc = collide(h);
+  if (rc) return rc;
+  if (n > 0) {
+    ReduceParams rp{};
+    rp.g = h->g;
+    rp.tab = h->tab;
+    rp.n = n;
+    rp.tag = tag;
+    rp.x = x;
+    rp.radius = r;
+    for (int d = 0; d < 3; ++d) rp.origin[d] = h->origin[d];
+    rp.dx = h->dx;
+    rp.forceFactor = h->forceFactor;
+    rp.torqueFactor = h->torqueFactor;
+    rp.nodeF_is_double = h->opt.storage == LBMPSM_STORAGE_FP64 ? 1 : 0;
+    rp.fh = h->d_out;
+    rp.th = h->d_out + 3 * (size_t)n;
+    rp.S = h->d_out + 6 * (size_t)n;
+    CUDA_TRY(h, launch_reduce(rp, h->stream));
+  }
+  h->last_n = n;
+  return LBMPSM_OK;
+}
+
+int enqueue_bc(lbmpsm_handle* h) {
+  if (h->faces.empty()) return LBMPSM_OK;
+  BCParams b{};
+  b.g = h->g;
+  b.f = h->f;
+  b.nfaces = (int)h->faces.size();
+  for (int k = 0; k < b.nfaces; ++k) b.face[k] = h->faces[k];
+  b.after_odd = (h->t % 2 == 0) ? 1 : 0;
+  b.scale16 = h->scale16;
+  cudaError_t e;
+  switch (h->opt.storage) {
+    case LBMPSM_STORAGE_FP64: e = launch_bc_f64(b, h->stream); break;
+    case LBMPSM_STORAGE_FP32: e = launch_bc_f32(b, h->stream); break;
+    default: e = launch_bc_f16(b, h->stream); break;
+  }
+  CUDA_TRY(h, e);
+  return LBMPSM_OK;
+}
+
+int read_status(lbmpsm_handle* h) {
+  int st = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (st & STATUS_LIST_OVERFLOW) {
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+    return fail(h, LBMPSM_ERR_CAPACITY,
+                "particle cell lists overflowed: a radius exceeds the handle's max_radius");
+  }
+  return LBMPSM_OK;
+}
+
+bool finite_all(const double* a, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(a[i])) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lbmpsm_last_error(const lbmpsm_handle* h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm_handle** out) {
+  if (!out) return fail(nullptr, LBMPSM_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (!p) return fail(nullptr, LBMPSM_ERR_ARG, "params is NULL");
+  // fix_LBM_PSM ctor checks (src/fix_LBM_PSM.cpp:15-83)
+  if (p->dimension != 2 && p->dimension != 3)
+    return fail(nullptr, LBMPSM_ERR_ARG, "Illegal fix lbm-psm command: dimension must be 2 or 3");
+  if (p->nevery <= 0 || p->Nlc <= 0 || !(p->lc > 0.0) || !(p->rho > 0.0) || !(p->nu > 0.0) ||
+      !(p->Re > 0.0) || !(p->tau > 0.5))
+    return fail(nullptr, LBMPSM_ERR_ARG, "Illegal fix lbm-psm command");
+  if (p->Nlc < 2) return fail(nullptr, LBMPSM_ERR_ARG, "Illegal fix lbm-psm command: Nlc must be > 1");
+  lbmpsm_options o{};
+  if (opts) o = *opts;
+  if (o.storage < 0 || o.storage > 2)
+    return fail(nullptr, LBMPSM_ERR_ARG, "unknown storage precision");
+  if (o.psm_weighting < 0 || o.psm_weighting > 1)
+    return fail(nullptr, LBMPSM_ERR_ARG, "unknown PSM weighting");
+
+  lbmpsm_handle* h = new (std::nothrow) lbmpsm_handle();
+  if (!h) return fail(nullptr, LBMPSM_ERR_NOMEM, "host allocation failed");
+  h->prm = *p;
+  h->opt = o;
+  // UnitConversion::UnitConversion (src/LBM_PSM_unitConversion.cpp:15-38)
+  {
+    const double Uc_d = 1.0, Lc_d = 1.0, csPow2 = 1.0 / 3.0;
+    const int N = p->Nlc;
+    h->nu_lb = (p->tau - 0.5) * csPow2;
+    h->dx = p->lc / (double)(N - 1);
+    h->dx_d = Lc_d / (double)(N - 1);
+    h->Uc = p->Re * p->nu / p->lc;
+    h->u_lb = p->Re * h->nu_lb / (double)(N - 1);
+    h->dt_d = h->dx_d * h->u_lb / Uc_d;
+    h->tc = p->lc / h->Uc;
+    h->forceFactor = p->rho * pow(p->lc, 4) / pow(h->tc, 2) * pow(h->dx_d, 4) / pow(h->dt_d, 2);
+    h->torqueFactor = p->rho * pow(p->lc, 5) / pow(h->tc, 2) * pow(h->dx_d, 5) / pow(h->dt_d, 2);
+    h->volumeForceFactor = p->rho * p->lc / pow(h->tc, 2) * h->dx_d / pow(h->dt_d, 2);
+  }
+  // fix_LBM_PSM::init checks (src/fix_LBM_PSM.cpp:122-140)
+  const double Ma = h->u_lb / (1.0 / sqrt(3.0));
+  if (Ma > 0.3) {
+    delete h;
+    return fail(nullptr, LBMPSM_ERR_MACH,
+                "Mach number is Ma > 0.3. Aborting simulation. Choose parameters which give Ma < "
+                "0.3 for stability reasons.");
+  }
+  const double SMALL = 1e-15, dx = h->dx;
+  if (pow(((double)((int)(p->prd[0] / dx + 0.5)) - p->prd[0] / dx), 2.0) > SMALL ||
+      pow(((double)((int)(p->prd[1] / dx + 0.5)) - p->prd[1] / dx), 2.0) > SMALL ||
+      pow(((double)((int)(p->prd[2] / dx + 0.5)) - p->prd[2] / dx), 2.0) > SMALL) {
+    delete h;
+    return fail(nullptr, LBMPSM_ERR_GRID,
+                "Illegal cell width. Division of domain length and cell width has to give an "
+                "integer.");
+  }
+  int gn[3];
+  gn[0] = p->prd[0] / dx + 1.5;
+  if (p->periodic[0]) gn[0] -= 1;
+  gn[1] = p->prd[1] / dx + 1.5;
+  if (p->periodic[1]) gn[1] -= 1;
+  gn[2] = 0;
+  if (p->dimension == 3) {
+    gn[2] = p->prd[2] / dx + 1.5;
+    if (p->periodic[2]) gn[2] -= 1;
+  }
+  for (int d = 0; d < p->dimension; ++d)
+    if (gn[d] < 1) {
+      delete h;
+      return fail(nullptr, LBMPSM_ERR_GRID, "lattice has no nodes along an axis");
+    }
+  h->origin[0] = p->boxlo[0];
+  h->origin[1] = p->boxlo[1];
+  h->origin[2] = p->dimension == 2 ? 0.0 : p->boxlo[2];
+  for (int d = 0; d < 3; ++d) h->F_lbm[d] = p->Fext[d] / h->volumeForceFactor;
+  h->has_force = (h->F_lbm[0] * h->F_lbm[0] + h->F_lbm[1] * h->F_lbm[1] + h->F_lbm[2] * h->F_lbm[2]) > 0.0;
+  h->tau = p->tau;
+  h->omega = 1.0 / p->tau;
+  {
+    const double csPow2 = 1.0 / 3.0, csPow4 = csPow2 * csPow2;
+    h->invCs2 = 1.0 / csPow2;
+    h->invCs4 = 1.0 / csPow4;
+  }
+  Geom& g = h->g;
+  g.dim = p->dimension;
+  g.Q = p->dimension == 2 ? 9 : 19;
+  for (int d = 0; d < 3; ++d) {
+    const bool real_axis = d < p->dimension;
+    g.L[d] = real_axis ? gn[d] + 2 : 1;
+    const bool per = !real_axis || p->periodic[d];
+    g.per[d] = per ? 1 : 0;
+    g.off[d] = (real_axis && per) ? 1 : 0;
+    g.S[d] = (real_axis && per) ? gn[d] : g.L[d];
+  }
+  g.N = (long long)g.S[0] * g.S[1] * g.S[2];
+  g.Np = (g.N + 63) / 64 * 64;
+  h->cb[0] = 8;
+  h->cb[1] = 8;
+  h->cb[2] = p->dimension == 3 ? 8 : 1;
+  for (int d = 0; d < 3; ++d) h->C[d] = (g.S[d] + h->cb[d] - 1) / h->cb[d];
+
+  h->device = o.device;
+  auto bail = [&](int rc) {
+    lbmpsm_destroy(h);
+    return fail(nullptr, rc, "device set-up failed: " + std::string(cudaGetErrorString(cudaGetLastError())));
+  };
+  if (cudaSetDevice(h->device) != cudaSuccess) return bail(LBMPSM_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(LBMPSM_ERR_CUDA);
+  const size_t es = storage_bytes(o.storage);
+  const size_t N = (size_t)g.N;
+  if (dmalloc(h, &h->f, es * (size_t)g.Np * g.Q) != cudaSuccess ||
+      dmalloc(h, &h->tab.flag, N) != cudaSuccess ||
+      dmalloc(h, &h->tab.ids, sizeof(int2) * N) != cudaSuccess ||
+      dmalloc(h, &h->tab.eps, sizeof(double2) * N) != cudaSuccess ||
+      dmalloc(h, &h->tab.us, sizeof(double) * 6 * N) != cudaSuccess ||
+      dmalloc(h, &h->tab.nodeF, (o.storage == 0 ? 8 : 4) * 6 * N) != cudaSuccess)
+    return bail(LBMPSM_ERR_NOMEM);
+  if (o.storage != 0 && dmalloc(h, &h->tab.rec32, sizeof(float4) * 2 * N) != cudaSuccess)
+    return bail(LBMPSM_ERR_NOMEM);
+  const int ncells = h->C[0] * h->C[1] * h->C[2];
+  if (dmalloc(h, &h->d_cells, sizeof(int) * 3 * (size_t)ncells) != cudaSuccess ||
+      dmalloc(h, &h->d_pair_total, sizeof(unsigned long long)) != cudaSuccess ||
+      dmalloc(h, &h->d_status, sizeof(int)) != cudaSuccess ||
+      dmalloc(h, &h->d_check, sizeof(double) * (4 + 4 * 1024)) != cudaSuccess)
+    return bail(LBMPSM_ERR_NOMEM);
+  cudaMemsetAsync(h->tab.flag, 0, N, h->stream);
+  cudaMemsetAsync(h->tab.ids, 0, sizeof(int2) * N, h->stream);
+  cudaMemsetAsync(h->tab.eps, 0, sizeof(double2) * N, h->stream);
+  cudaMemsetAsync(h->tab.us, 0, sizeof(double) * 6 * N, h->stream);
+  cudaMemsetAsync(h->tab.nodeF, 0, (o.storage == 0 ? 8 : 4) * 6 * N, h->stream);
+  if (h->tab.rec32) cudaMemsetAsync(h->tab.rec32, 0, sizeof(float4) * 2 * N, h->stream);
+  cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream);
+  if (launch_init_populations(g, h->f, o.storage, h->scale16, h->stream) != cudaSuccess)
+    return bail(LBMPSM_ERR_CUDA);
+  int rc = ensure_particles(h, std::max(o.max_images, 1), o.max_radius > 0 ? o.max_radius : 8.0 * h->dx);
+  if (rc) {
+    std::string m = h->err;
+    lbmpsm_destroy(h);
+    return fail(nullptr, rc, m);
+  }
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(LBMPSM_ERR_CUDA);
+  *out = h;
+  return LBMPSM_OK;
+}
+
+void lbmpsm_destroy(lbmpsm_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
+  free_particles(h);
+  dfree(h->f);
+  dfree(h->tab.flag);
+  dfree(h->tab.ids);
+  dfree(h->tab.eps);
+  dfree(h->tab.us);
+  dfree(h->tab.rec32);
+  dfree(h->tab.nodeF);
+  dfree(h->rho);
+  dfree(h->u);
+  dfree(h->d_cells);
+  dfree(h->d_pair_total);
+  dfree(h->d_status);
+  dfree(h->d_check);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int lbmpsm_get_info(const lbmpsm_handle* h, lbmpsm_info* info) {
+  if (!h || !info) return LBMPSM_ERR_ARG;
+  info->dimension = h->g.dim;
+  info->q = h->g.Q;
+  info->nx = h->g.L[0] - 2;
+  info->ny = h->g.L[1] - 2;
+  info->nz = h->g.dim == 3 ? h->g.L[2] - 2 : 0;
+  for (int d = 0; d < 3; ++d) {
+    info->local[d] = h->g.L[d];
+    info->storage_dims[d] = h->g.S[d];
+  }
+  info->dx = h->dx;
+  info->Uc = h->Uc;
+  info->u_lb = h->u_lb;
+  info->tc = h->tc;
+  info->dt_d = h->dt_d;
+  info->forceFactor = h->forceFactor;
+  info->torqueFactor = h->torqueFactor;
+  info->volumeForceFactor = h->volumeForceFactor;
+  info->dt_dem = (1.0 * h->dt_d * h->tc) / ((double)h->prm.nevery);
+  info->Ma = h->u_lb / (1.0 / sqrt(3.0));
+  for (int d = 0; d < 3; ++d) info->F_lbm[d] = h->F_lbm[d];
+  info->steps = h->t;
+  info->device_bytes = h->dev_bytes;
+  return LBMPSM_OK;
+}
+
+int lbmpsm_set_bc(lbmpsm_handle* h, int bc_type) {
+  if (!h) return LBMPSM_ERR_ARG;
+  if (bc_type < 0 || bc_type > 5) return fail(h, LBMPSM_ERR_ARG, "Illegal fix lbm-psm-bc command");
+  h->bc_type = bc_type;
+  make_faces(h, bc_type);
+  drop_graphs(h);
+  return LBMPSM_OK;
+}
+
+int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
+                const double* omega, const double* radius, double* fh, double* th,
+                double* stresslet) {
+  if (!h || n < 0) return LBMPSM_ERR_ARG;
+  if (n > 0 && (!tag || !x || !v || !omega || !radius || !fh || !th || !stresslet))
+    return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  double rmax = 0.0;
+  for (int i = 0; i < n; ++i) rmax = std::max(rmax, radius[i]);
+  if (!finite_all(x, 3 * (size_t)n) || !std::isfinite(rmax))
+    return fail(h, LBMPSM_ERR_NUMERIC, "non-finite particle position or radius");
+  int rc = ensure_particles(h, n, std::max(rmax, h->opt.max_radius));
+  if (rc) return rc;
+  if (n > 0) {
+    // pinned staging: tags, then x | v | omega | radius; two copies to the device
+    const size_t cap = (size_t)h->cap;
+    char* st = static_cast<char*>(h->h_stage);
+    int* stag = reinterpret_cast<int*>(st);
+    double* sx = reinterpret_cast<double*>(st + ((sizeof(int) * cap + 15) & ~(size_t)15));
+    const size_t nn = (size_t)n;
+    std::memcpy(stag, tag, sizeof(int) * nn);
+    std::memcpy(sx, x, sizeof(double) * 3 * nn);
+    std::memcpy(sx + 3 * nn, v, sizeof(double) * 3 * nn);
+    std::memcpy(sx + 6 * nn, omega, sizeof(double) * 3 * nn);
+    std::memcpy(sx + 9 * nn, radius, sizeof(double) * nn);
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_tag, stag, sizeof(int) * nn, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw, sx, sizeof(double) * 10 * nn, cudaMemcpyHostToDevice,
+                                h->stream));
+  }
+  rc = enqueue_step(h, n);
+  if (rc) return rc;
+  if (n > 0) {
+    double* out = reinterpret_cast<double*>(static_cast<char*>(h->h_stage) +
+                                            ((sizeof(int) * h->cap + 15) & ~(size_t)15) +
+                                            sizeof(double) * 10 * (size_t)h->cap);
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->d_out, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost,
+                                h->stream));
+    rc = read_status(h);  // synchronises
+    if (rc) return rc;
+    std::memcpy(fh, out, sizeof(double) * 3 * n);
+    std::memcpy(th, out + 3 * n, sizeof(double) * 3 * n);
+    std::memcpy(stresslet, out + 6 * n, sizeof(double) * 6 * n);
+  } else {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  }
+  return LBMPSM_OK;
+}
+
+int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
+                       const double* omega, const double* radius, double* fh, double* th,
+                       double* stresslet) {
+  if (!h || n < 0) return LBMPSM_ERR_ARG;
+  if (n > h->cap) return fail(h, LBMPSM_ERR_CAPACITY, "more images than options.max_images");
+  if (h->opt.max_radius <= 0.0)
+    return fail(h, LBMPSM_ERR_ARG, "lbmpsm_step_device needs options.max_radius");
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  const size_t nn = (size_t)n;
+  if (n > 0) {
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_tag, tag, sizeof(int) * nn, cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw, x, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw + 3 * nn, v, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw + 6 * nn, omega, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw + 9 * nn, radius, sizeof(double) * nn, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  int rc = enqueue_step(h, n);
+  if (rc) return rc;
+  if (n > 0) {
+    if (fh) CUDA_TRY(h, cudaMemcpyAsync(fh, h->d_out, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, h->stream));
+    if (th) CUDA_TRY(h, cudaMemcpyAsync(th, h->d_out + 3 * (size_t)n, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, h->stream));
+    if (stresslet) CUDA_TRY(h, cudaMemcpyAsync(stresslet, h->d_out + 6 * (size_t)n, sizeof(double) * 6 * n, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  return LBMPSM_OK;
+}
+
+int lbmpsm_apply_bc(lbmpsm_handle* h) {
+  if (!h) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  return enqueue_bc(h);
+}
+
+int lbmpsm_request_macro(lbmpsm_handle* h) {
+  if (!h) return LBMPSM_ERR_ARG;
+  if (!h->rho) {
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, dmalloc(h, &h->rho, sizeof(double) * (size_t)h->g.N));
+    CUDA_TRY(h, dmalloc(h, &h->u, sizeof(double) * 3 * (size_t)h->g.N));
+    drop_graphs(h);
+  }
+  h->macro_requested = true;
+  return LBMPSM_OK;
+}
+
+int lbmpsm_export_fields(lbmpsm_handle* h, int as_double, double B0, double rho0, double u0,
+                         void* solid, void* rho, void* u) {
+  if (!h) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  const Geom& g = h->g;
+  const size_t npts = (size_t)(g.L[0] - 2) * (g.L[1] - 2) * (g.dim == 3 ? g.L[2] - 2 : 1);
+  const size_t es = as_double ? 8 : 4;
+  void* d = nullptr;
+  CUDA_TRY(h, cudaMalloc(&d, es * 5 * npts));
+  char* b = static_cast<char*>(d);
+  cudaError_t e = launch_export_fields(g, h->tab, h->macro_valid ? h->rho : nullptr,
+                                       h->macro_valid ? h->u : nullptr, as_double, B0, rho0, u0, b,
+                                       b + es * npts, b + 2 * es * npts, h->stream);
+  if (e == cudaSuccess && solid) e = cudaMemcpyAsync(solid, b, es * npts, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && rho) e = cudaMemcpyAsync(rho, b + es * npts, es * npts, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, b + 2 * es * npts, 3 * es * npts, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  CUDA_TRY(h, e);
+  return LBMPSM_OK;
+}
+
+int lbmpsm_get_populations(lbmpsm_handle* h, double* f) {
+  if (!h || !f) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  const Geom& g = h->g;
+  const size_t cnt = (size_t)g.L[0] * g.L[1] * g.L[2] * g.Q;
+  double* d = nullptr;
+  CUDA_TRY(h, cudaMalloc(&d, sizeof(double) * cnt));
+  cudaError_t e = launch_get_populations(g, h->f, h->opt.storage, (h->t % 2 == 0) ? 1 : 0,
+                                         h->scale16, d, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(f, d, sizeof(double) * cnt, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  CUDA_TRY(h, e);
+  return LBMPSM_OK;
+}
+
+int lbmpsm_set_populations(lbmpsm_handle* h, const double* f) {
+  if (!h || !f) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  const Geom& g = h->g;
+  const size_t cnt = (size_t)g.L[0] * g.L[1] * g.L[2] * g.Q;
+  double* d = nullptr;
+  CUDA_TRY(h, cudaMalloc(&d, sizeof(double) * cnt));
+  cudaError_t e = cudaMemcpyAsync(d, f, sizeof(double) * cnt, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = launch_set_populations(g, h->f, h->opt.storage, (h->t % 2 == 0) ? 1 : 0, h->scale16, d,
+                               h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  CUDA_TRY(h, e);
+  return LBMPSM_OK;
+}
+
+int lbmpsm_get_particle_table(lbmpsm_handle* h, int* ids, double* eps, double* us) {
+  if (!h) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  const Geom& g = h->g;
+  const size_t N = (size_t)g.L[0] * g.L[1] * g.L[2];
+  void* d = nullptr;
+  CUDA_TRY(h, cudaMalloc(&d, N * (2 * sizeof(int) + 8 * sizeof(double))));
+  int* di = static_cast<int*>(d);
+  double* de = reinterpret_cast<double*>(di + 2 * N);
+  double* du = de + 2 * N;
+  cudaError_t e = launch_table_export(g, h->tab, di, de, du, h->stream);
+  if (e == cudaSuccess && ids) e = cudaMemcpyAsync(ids, di, sizeof(int) * 2 * N, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && eps) e = cudaMemcpyAsync(eps, de, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && us) e = cudaMemcpyAsync(us, du, sizeof(double) * 6 * N, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  CUDA_TRY(h, e);
+  return LBMPSM_OK;
+}
+
+int lbmpsm_check(lbmpsm_handle* h, double* mass, double* momentum3) {
+  if (!h) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  CUDA_TRY(h, launch_check(h->g, h->f, h->opt.storage, (h->t % 2 == 0) ? 1 : 0, h->scale16,
+                           h->d_check, h->d_status, h->stream));
+  double acc[4];
+  int st = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(acc, h->d_check, sizeof(acc), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (mass) *mass = acc[0];
+  if (momentum3)
+    for (int d = 0; d < 3; ++d) momentum3[d] = acc[1 + d];
+  if (st & STATUS_NONFINITE) {
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+    return fail(h, LBMPSM_ERR_NUMERIC, "non-finite populations detected");
+  }
+  return LBMPSM_OK;
+}
+
+int lbmpsm_synchronize(lbmpsm_handle* h) {
+  if (!h) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return read_status(h);
+}
+
+void* lbmpsm_stream(lbmpsm_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps) {
+  if (!h || nsteps < 0) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  const int n = h->last_n;
+  const int use_bc = h->faces.empty() ? 0 : 1;
+  if (h->graph_n != n || h->graph_bc != use_bc || h->macro_requested) drop_graphs(h);
+  // a requested macro store runs eagerly (it changes the kernel arguments)
+  while (nsteps > 0 && h->macro_requested) {
+    int rc = enqueue_step(h, n);
+    if (!rc && use_bc) rc = enqueue_bc(h);
+    if (rc) return rc;
+    --nsteps;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    const int par = (int)(h->t & 1);
+    if (!h->gexec[par]) {
+      cudaGraph_t graph;
+      CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      const long long t0 = h->t;
+      int rc = enqueue_step(h, n);
+      if (!rc && use_bc) rc = enqueue_bc(h);
+      cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+      h->t = t0;  // captured, not run
+      if (rc) return rc;
+      CUDA_TRY(h, ce);
+      cudaError_t ie = cudaGraphInstantiate(&h->gexec[par], graph, 0);
+      cudaGraphDestroy(graph);
+      CUDA_TRY(h, ie);
+      h->graph_n = n;
+      h->graph_bc = use_bc;
+    }
+    CUDA_TRY(h, cudaGraphLaunch(h->gexec[par], h->stream));
+    h->t += 1;
+  }
+  return LBMPSM_OK;
+}
+
+int lbmpsm_read_forces(lbmpsm_handle* h, int n, double* fh, double* th, double* stresslet) {
+  if (!h || n < 0 || n > h->last_n) return LBMPSM_ERR_ARG;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  const size_t m = (size_t)h->last_n;
+  if (fh) CUDA_TRY(h, cudaMemcpyAsync(fh, h->d_out, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+  if (th) CUDA_TRY(h, cudaMemcpyAsync(th, h->d_out + 3 * m, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+  if (stresslet) CUDA_TRY(h, cudaMemcpyAsync(stresslet, h->d_out + 6 * m, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return read_status(h);
+}
+
+}  // extern "C"

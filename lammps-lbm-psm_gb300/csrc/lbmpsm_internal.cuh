@@ -1,0 +1,270 @@
+// lbmpsm_internal.cuh -- shared definitions of the GB300 LBM-PSM library.
+//
+// Device data layout (one lattice = one handle):
+//   populations  SoA, f[q*Np + node], node = (sz*S1 + sy)*S0 + sx, x fastest.
+//                In-place "A-A" streaming: even steps read and write a node's
+//                own slots (writing direction q into slot opp(q)), odd steps
+//                gather from and scatter to the neighbours.  One copy of the
+//                populations, every population read once and written once per
+//                step.
+//   storage extents S[d]: periodic axes hold only the n interior nodes and
+//                wrap; non-periodic axes also hold the two halo planes of the
+//                reference lattice (which collides them and whose populations
+//                streamed in from outside the array stay at the initial
+//                equilibrium w_q).  Reference halo index h = s + off[d].
+//   particle table per node (the reference's ParticleDataOnLattice without
+//                its force slots): flag (bit0/bit1 = slot occupied), ids,
+//                eps, us in FP64, and an FP32 mirror for the FP32/FP16
+//                collision kernels.  Node forces of the current step are
+//                written per PSM node and reduced per particle image.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lbmpsm {
+
+// ---------------------------------------------------------------- lattices
+// Velocity sets and weights of src/LBM_PSM_lattice.h:186-209.
+struct D2Q9 {
+  static constexpr int Q = 9;
+  static constexpr int DIM = 2;
+  __host__ __device__ static constexpr int ex(int q) {
+    return (q == 1 || q == 5 || q == 8) ? 1 : ((q == 3 || q == 6 || q == 7) ? -1 : 0);
+  }
+  __host__ __device__ static constexpr int ey(int q) {
+    return (q == 2 || q == 5 || q == 6) ? 1 : ((q == 4 || q == 7 || q == 8) ? -1 : 0);
+  }
+  __host__ __device__ static constexpr int ez(int) { return 0; }
+  __host__ __device__ static constexpr int opp(int q) {
+    return q == 0 ? 0 : (q <= 4 ? ((q + 1) % 4) + 1 : ((q - 5 + 2) % 4) + 5);
+  }
+  __host__ __device__ static constexpr double w(int q) {
+    return q == 0 ? 4.0 / 9.0 : (q <= 4 ? 1.0 / 9.0 : 1.0 / 36.0);
+  }
+};
+
+struct D3Q19 {
+  static constexpr int Q = 19;
+  static constexpr int DIM = 3;
+  __host__ __device__ static constexpr int ex(int q) {
+    return (q == 1 || q == 7 || q == 9 || q == 13 || q == 15)
+               ? 1
+               : ((q == 2 || q == 8 || q == 10 || q == 14 || q == 16) ? -1 : 0);
+  }
+  __host__ __device__ static constexpr int ey(int q) {
+    return (q == 3 || q == 7 || q == 11 || q == 14 || q == 17)
+               ? 1
+               : ((q == 4 || q == 8 || q == 12 || q == 13 || q == 18) ? -1 : 0);
+  }
+  __host__ __device__ static constexpr int ez(int q) {
+    return (q == 5 || q == 9 || q == 11 || q == 16 || q == 18)
+               ? 1
+               : ((q == 6 || q == 10 || q == 12 || q == 15 || q == 17) ? -1 : 0);
+  }
+  __host__ __device__ static constexpr int opp(int q) {
+    return q == 0 ? 0 : ((q & 1) ? q + 1 : q - 1);
+  }
+  __host__ __device__ static constexpr double w(int q) {
+    return q == 0 ? 1.0 / 3.0 : (q <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
+  }
+};
+
+// ---------------------------------------------------------------- geometry
+struct Geom {
+  int dim, Q;
+  int L[3];    // reference local sizes including halo (L[2] = 1 in 2-D)
+  int S[3];    // device storage extents
+  int off[3];  // reference index h = s + off
+  int per[3];  // periodic axes wrap; the 2-D z axis counts as periodic
+  long long N; // S0*S1*S2
+  long long Np;// population stride (N rounded up to 64)
+};
+
+// Neighbour offsets of one node: o[axis][0] towards -1, o[axis][1] towards +1
+// (in nodes); v bit (2*axis + side) set when that neighbour exists.
+struct Nbr {
+  int o[3][2];
+  unsigned v;
+};
+
+__device__ __forceinline__ Nbr make_nbr(const Geom& g, int sx, int sy, int sz) {
+  Nbr nb;
+  nb.v = 0;
+  const int s[3] = {sx, sy, sz};
+  const int stride[3] = {1, g.S[0], g.S[0] * g.S[1]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int n = g.S[a];
+    // towards -1
+    if (s[a] > 0) {
+      nb.o[a][0] = -stride[a];
+      nb.v |= 1u << (2 * a);
+    } else if (g.per[a]) {
+      nb.o[a][0] = (n - 1) * stride[a];
+      nb.v |= 1u << (2 * a);
+    } else {
+      nb.o[a][0] = 0;
+    }
+    // towards +1
+    if (s[a] < n - 1) {
+      nb.o[a][1] = stride[a];
+      nb.v |= 1u << (2 * a + 1);
+    } else if (g.per[a]) {
+      nb.o[a][1] = -(n - 1) * stride[a];
+      nb.v |= 1u << (2 * a + 1);
+    } else {
+      nb.o[a][1] = 0;
+    }
+  }
+  return nb;
+}
+
+// offset and existence of the neighbour in direction (cx, cy, cz), c in {-1,0,1}
+__device__ __forceinline__ int nbr_off(const Nbr& nb, int cx, int cy, int cz) {
+  int o = 0;
+  if (cx) o += nb.o[0][cx > 0];
+  if (cy) o += nb.o[1][cy > 0];
+  if (cz) o += nb.o[2][cz > 0];
+  return o;
+}
+__device__ __forceinline__ bool nbr_ok(const Nbr& nb, int cx, int cy, int cz) {
+  bool ok = true;
+  if (cx) ok = ok && ((nb.v >> (0 + (cx > 0))) & 1u);
+  if (cy) ok = ok && ((nb.v >> (2 + (cy > 0))) & 1u);
+  if (cz) ok = ok && ((nb.v >> (4 + (cz > 0))) & 1u);
+  return ok;
+}
+
+// ---------------------------------------------------------------- particle table
+struct Table {
+  uint8_t* flag;   // N
+  int2* ids;       // N
+  double2* eps;    // N
+  double* us;      // 6N  (slot-major: us[6n + 3*slot + c])
+  float4* rec32;   // 2N  (eps, usx, usy, usz) per slot, FP32 mirror
+  void* nodeF;     // 6N  FP64 (FP64 storage) or FP32 (other storages)
+};
+
+// ---------------------------------------------------------------- step params
+struct CollideParams {
+  Geom g;
+  void* f;                // populations (double / float / half)
+  Table tab;
+  double* rho_out;        // optional macro output (N), FP64
+  double* u_out;          // optional (3N)
+  int store_macro;
+  int weighting;          // LBMPSM_WEIGHT_*
+  double tau, omega, one_minus_omega, guo_pref;
+  double F[3];
+  int has_force;          // |F_lbm|^2 > 0
+  double invCs2, invCs4;
+  float scale16;          // FP16 storage: stored value = deviation * scale16
+};
+
+// Zou-He face list of one `fix lbm-psm-bc` keyword.
+enum FaceKind {
+  FACE_VEL2_XN, FACE_VEL2_XP, FACE_DENS2_XP, FACE_VEL2_YN, FACE_VEL2_YP,
+  FACE_VEL3_XN, FACE_VEL3_XP, FACE_DENS3_XP, FACE_VEL3_YN, FACE_VEL3_YP,
+  FACE_VEL3_ZN, FACE_VEL3_ZP
+};
+struct Face {
+  int kind;
+  int axis;        // normal axis
+  int plane;       // storage index of the face plane along axis
+  int lo[3], hi[3];// inclusive storage ranges of the face nodes (axis: plane..plane)
+  double p0;       // velocity (vel faces) or density (dens faces)
+};
+struct BCParams {
+  Geom g;
+  void* f;
+  int nfaces;
+  Face face[6];
+  int after_odd;   // 1: the last step was odd (natural layout), 0: even (swapped layout)
+  float scale16;
+};
+
+// ---------------------------------------------------------------- particles
+struct Img {
+  int tag;
+  int valid;          // box non-empty on the device lattice
+  int lo[3], hi[3];   // map box, storage coordinates, [lo, hi)
+  int clo[3], chi[3]; // cell range touched, inclusive
+  double xl[3];       // lattice-local centre (reference halo frame)
+  double r;           // radius, lattice units
+  double uT[3];       // translational velocity, lattice units
+  double om[3];       // angular velocity, lattice units
+};
+
+struct MapParams {
+  Geom g;
+  Table tab;
+  int n;
+  const int* tag;
+  const double* x;
+  const double* v;
+  const double* omega;
+  const double* radius;
+  double origin[3];
+  double dx, Uc, u_lb, tc, dt_d;
+  double sqrt2half;   // sqrt(2.1)/2 in 2-D, sqrt(3.1)/2 in 3-D (host libm)
+  Img* img;
+  int cb[3];          // cell edge (nodes) per axis
+  int C[3];           // cells per axis
+  int* cell_count;
+  int* cell_off;
+  int* cell_fill;
+  int* list;
+  long long list_cap;
+  unsigned long long* pair_total;
+  int* status;
+  int write32;        // also write the FP32 mirror
+};
+
+struct ReduceParams {
+  Geom g;
+  Table tab;
+  int n;
+  const int* tag;
+  const double* x;
+  const double* radius;
+  double origin[3];
+  double dx;
+  double forceFactor, torqueFactor;
+  int nodeF_is_double;
+  double* fh;
+  double* th;
+  double* S;
+};
+
+// status bits
+enum : int { STATUS_LIST_OVERFLOW = 1, STATUS_NONFINITE = 2 };
+
+// ---------------------------------------------------------------- launchers
+// collide.cu / collide_f32.cu
+cudaError_t launch_collide_f64(const CollideParams& p, int odd, cudaStream_t st);
+cudaError_t launch_collide_f32(const CollideParams& p, int odd, cudaStream_t st);
+cudaError_t launch_collide_f16(const CollideParams& p, int odd, cudaStream_t st);
+cudaError_t launch_bc_f64(const BCParams& p, cudaStream_t st);
+cudaError_t launch_bc_f32(const BCParams& p, cudaStream_t st);
+cudaError_t launch_bc_f16(const BCParams& p, cudaStream_t st);
+// population layout conversions (storage <-> reference AoS with halo, FP64)
+cudaError_t launch_init_populations(const Geom& g, void* f, int storage, float scale16,
+                                    cudaStream_t st);
+cudaError_t launch_get_populations(const Geom& g, const void* f, int storage, int after_odd,
+                                   float scale16, double* out_ref, cudaStream_t st);
+cudaError_t launch_set_populations(const Geom& g, void* f, int storage, int after_odd,
+                                   float scale16, const double* in_ref, cudaStream_t st);
+cudaError_t launch_check(const Geom& g, const void* f, int storage, int after_odd,
+                         float scale16, double* acc4, int* status, cudaStream_t st);
+// particles.cu
+cudaError_t launch_map(const MapParams& p, cudaStream_t st);
+cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st);
+cudaError_t launch_table_export(const Geom& g, const Table& t, int* ids, double* eps,
+                                double* us, cudaStream_t st);
+cudaError_t launch_export_fields(const Geom& g, const Table& t, const double* rho,
+                                 const double* u, int as_double, double B0, double rho0,
+                                 double u0, void* solid_out, void* rho_out, void* u_out,
+                                 cudaStream_t st);
+
+}  // namespace lbmpsm

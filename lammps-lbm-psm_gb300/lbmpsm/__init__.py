@@ -1,0 +1,276 @@
+"""Python binding of liblbmpsm_gb300.so (the C ABI in include/lbmpsm.h).
+
+``Lattice`` is one ``fix lbm-psm`` lattice resident on a GPU.  Its methods map
+one-to-one onto the library's entry points, which replace the reference's
+call sites (timnajuch/LAMMPS-LBM-PSM):
+
+    Lattice(...)          fix_LBM_PSM::init              src/fix_LBM_PSM.cpp:104-177
+    Lattice.set_bc(kw)    fix lbm-psm-bc keyword + init  src/fix_LBM_PSM_BC.cpp:16-39,145-148
+    Lattice.step(...)     LBM branch of post_force        src/fix_LBM_PSM.cpp:197-229
+    Lattice.apply_bc()    fix_LBM_PSM_BC::post_force     src/fix_LBM_PSM_BC.cpp:151-402
+    Lattice.export_fields execute_write_vti field read   src/fix_LBM_PSM_writeVTI.h:146-169
+
+There is no CPU fallback: constructing a ``Lattice`` without the built library
+or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .host import FixLbmPsm, FixLbmPsmBC, FixLbmPsmVTI, LammpsError, ghost_images, reverse_comm  # noqa: F401
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "liblbmpsm_gb300.so")
+
+OK = 0
+ERR_ARG, ERR_MACH, ERR_GRID, ERR_NOMEM, ERR_CUDA, ERR_STATE, ERR_CAPACITY, ERR_NUMERIC, ERR_TIMEOUT = (
+    -1, -2, -3, -4, -5, -6, -7, -8, -9)
+STORAGE = {"fp64": 0, "fp32": 1, "fp16": 2}
+BC = {"none": 0, "shear": 1, "xFlow": 2, "channel": 3, "channel-velIn-pressOut": 4, "closedBox": 5}
+WEIGHTING = {"reference": 0, "noble-torczynski": 1}
+
+SYMBOLS = (
+    "lbmpsm_create", "lbmpsm_destroy", "lbmpsm_last_error", "lbmpsm_get_info", "lbmpsm_set_bc",
+    "lbmpsm_step", "lbmpsm_step_device", "lbmpsm_apply_bc", "lbmpsm_request_macro",
+    "lbmpsm_export_fields", "lbmpsm_get_populations", "lbmpsm_set_populations",
+    "lbmpsm_get_particle_table", "lbmpsm_check", "lbmpsm_synchronize", "lbmpsm_stream",
+    "lbmpsm_run_fixed", "lbmpsm_read_forces",
+)
+
+
+class LbmPsmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class FixParams(C.Structure):
+    _fields_ = [
+        ("dimension", C.c_int), ("boxlo", C.c_double * 3), ("prd", C.c_double * 3),
+        ("periodic", C.c_int * 3), ("nevery", C.c_int), ("Nlc", C.c_int), ("lc", C.c_double),
+        ("rho", C.c_double), ("nu", C.c_double), ("Re", C.c_double), ("tau", C.c_double),
+        ("Fext", C.c_double * 3),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("storage", C.c_int), ("device", C.c_int), ("max_images", C.c_int),
+        ("max_radius", C.c_double), ("psm_weighting", C.c_int),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("dimension", C.c_int), ("q", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("local", C.c_int * 3), ("storage_dims", C.c_int * 3),
+        ("dx", C.c_double), ("Uc", C.c_double), ("u_lb", C.c_double), ("tc", C.c_double),
+        ("dt_d", C.c_double), ("forceFactor", C.c_double), ("torqueFactor", C.c_double),
+        ("volumeForceFactor", C.c_double), ("dt_dem", C.c_double), ("Ma", C.c_double),
+        ("F_lbm", C.c_double * 3), ("steps", C.c_int64), ("device_bytes", C.c_size_t),
+    ]
+
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_lib: C.CDLL | None = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"liblbmpsm_gb300.so not found at {path}: run lammps-lbm-psm_gb300/build.py")
+    lib = C.CDLL(path)
+    H = C.c_void_p
+    lib.lbmpsm_create.argtypes = [C.POINTER(FixParams), C.POINTER(Options), C.POINTER(H)]
+    lib.lbmpsm_destroy.argtypes = [H]
+    lib.lbmpsm_destroy.restype = None
+    lib.lbmpsm_last_error.argtypes = [H]
+    lib.lbmpsm_last_error.restype = C.c_char_p
+    lib.lbmpsm_get_info.argtypes = [H, C.POINTER(Info)]
+    lib.lbmpsm_set_bc.argtypes = [H, C.c_int]
+    lib.lbmpsm_step.argtypes = [H, C.c_int, _I, _D, _D, _D, _D, _D, _D, _D]
+    lib.lbmpsm_step_device.argtypes = [H, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.lbmpsm_apply_bc.argtypes = [H]
+    lib.lbmpsm_request_macro.argtypes = [H]
+    lib.lbmpsm_export_fields.argtypes = [H, C.c_int, C.c_double, C.c_double, C.c_double,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.lbmpsm_get_populations.argtypes = [H, _D]
+    lib.lbmpsm_set_populations.argtypes = [H, _D]
+    lib.lbmpsm_get_particle_table.argtypes = [H, _I, _D, _D]
+    lib.lbmpsm_check.argtypes = [H, _D, _D]
+    lib.lbmpsm_synchronize.argtypes = [H]
+    lib.lbmpsm_stream.argtypes = [H]
+    lib.lbmpsm_stream.restype = C.c_void_p
+    lib.lbmpsm_run_fixed.argtypes = [H, C.c_int]
+    lib.lbmpsm_read_forces.argtypes = [H, C.c_int, _D, _D, _D]
+    _lib = lib
+    return lib
+
+
+def _p(a, t=_D):
+    return a.ctypes.data_as(t)
+
+
+class Lattice:
+    """One LBM-PSM lattice on a GPU (a `fix lbm-psm` instance)."""
+
+    def __init__(self, *, dimension: int = 3, boxlo=(0.0, 0.0, 0.0), prd, periodic=(1, 1, 1),
+                 nevery: int = 1, Nlc: int, lc: float, rho: float = 1.0, nu: float, Re: float,
+                 tau: float = 0.7, Fext=(0.0, 0.0, 0.0), storage: str = "fp64", device: int = 0,
+                 max_images: int = 0, max_radius: float = 0.0, weighting: str = "reference",
+                 bc: str | int = "none"):
+        self.lib = load()
+        p = FixParams()
+        p.dimension = dimension
+        p.boxlo = (C.c_double * 3)(*boxlo)
+        p.prd = (C.c_double * 3)(*prd)
+        p.periodic = (C.c_int * 3)(*[int(v) for v in periodic])
+        p.nevery, p.Nlc, p.lc, p.rho, p.nu, p.Re, p.tau = nevery, Nlc, lc, rho, nu, Re, tau
+        p.Fext = (C.c_double * 3)(*Fext)
+        o = Options()
+        o.storage = STORAGE[storage]
+        o.device = device
+        o.max_images = max_images
+        o.max_radius = max_radius
+        o.psm_weighting = WEIGHTING[weighting]
+        h = C.c_void_p()
+        rc = self.lib.lbmpsm_create(C.byref(p), C.byref(o), C.byref(h))
+        if rc != OK:
+            raise LbmPsmError(rc, self.lib.lbmpsm_last_error(None).decode())
+        self.h = h
+        self.dimension = dimension
+        self.storage = storage
+        self.origin = (float(boxlo[0]), float(boxlo[1]), float(boxlo[2]) if dimension == 3 else 0.0)
+        self.info = self.get_info()
+        self.local = tuple(self.info.local)
+        self.q = self.info.q
+        if bc not in ("none", 0):
+            self.set_bc(bc)
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbmpsm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != OK:
+            raise LbmPsmError(rc, self.lib.lbmpsm_last_error(self.h).decode())
+
+    def get_info(self) -> Info:
+        info = Info()
+        self._check(self.lib.lbmpsm_get_info(self.h, C.byref(info)))
+        return info
+
+    @property
+    def steps(self) -> int:
+        return int(self.get_info().steps)
+
+    # -- the coupling step
+    def set_bc(self, kind):
+        self._check(self.lib.lbmpsm_set_bc(self.h, BC[kind] if isinstance(kind, str) else int(kind)))
+
+    def step(self, tag, x, v, omega, radius):
+        tag = np.ascontiguousarray(tag, dtype=np.int32)
+        n = len(tag)
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(n, 3)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(n, 3)
+        omega = np.ascontiguousarray(omega, dtype=np.float64).reshape(n, 3)
+        radius = np.ascontiguousarray(radius, dtype=np.float64).reshape(n)
+        fh = np.zeros((n, 3)); th = np.zeros((n, 3)); S = np.zeros((n, 6))
+        self._check(self.lib.lbmpsm_step(self.h, n, _p(tag, _I), _p(x), _p(v), _p(omega),
+                                         _p(radius), _p(fh), _p(th), _p(S)))
+        return fh, th, S
+
+    def step_device(self, n, tag_ptr, x_ptr, v_ptr, omega_ptr, radius_ptr, fh_ptr=None,
+                    th_ptr=None, s_ptr=None):
+        self._check(self.lib.lbmpsm_step_device(self.h, int(n), tag_ptr, x_ptr, v_ptr, omega_ptr,
+                                                radius_ptr, fh_ptr, th_ptr, s_ptr))
+
+    def apply_bc(self):
+        self._check(self.lib.lbmpsm_apply_bc(self.h))
+
+    def run_fixed(self, nsteps: int):
+        self._check(self.lib.lbmpsm_run_fixed(self.h, int(nsteps)))
+
+    def read_forces(self, n: int):
+        fh = np.zeros((n, 3)); th = np.zeros((n, 3)); S = np.zeros((n, 6))
+        self._check(self.lib.lbmpsm_read_forces(self.h, n, _p(fh), _p(th), _p(S)))
+        return fh, th, S
+
+    def synchronize(self):
+        self._check(self.lib.lbmpsm_synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.lbmpsm_stream(self.h) or 0)
+
+    # -- fields and state
+    def request_macro(self):
+        self._check(self.lib.lbmpsm_request_macro(self.h))
+
+    def export_fields(self, B0=1.0, rho0=1.0, u0=1.0, as_double=True):
+        nx, ny, nz = self.local
+        npts = (nx - 2) * (ny - 2) * ((nz - 2) if self.dimension == 3 else 1)
+        dt = np.float64 if as_double else np.float32
+        solid = np.empty(npts, dt); rho = np.empty(npts, dt); u = np.empty((npts, 3), dt)
+        self._check(self.lib.lbmpsm_export_fields(self.h, int(as_double), B0, rho0, u0,
+                                                  solid.ctypes.data, rho.ctypes.data, u.ctypes.data))
+        return solid, rho, u
+
+    def populations(self) -> np.ndarray:
+        f = np.empty(self.local + (self.q,), dtype=np.float64)
+        self._check(self.lib.lbmpsm_get_populations(self.h, _p(f)))
+        return f
+
+    def set_populations(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.local + (self.q,))
+        self._check(self.lib.lbmpsm_set_populations(self.h, _p(f)))
+
+    def particle_table(self):
+        N = int(np.prod(self.local))
+        ids = np.empty((N, 2), np.int32); eps = np.empty((N, 2)); us = np.empty((N, 6))
+        self._check(self.lib.lbmpsm_get_particle_table(self.h, _p(ids, _I), _p(eps), _p(us)))
+        s = self.local
+        return ids.reshape(s + (2,)), eps.reshape(s + (2,)), us.reshape(s + (6,))
+
+    def check(self):
+        mass = C.c_double(); mom = (C.c_double * 3)()
+        rc = self.lib.lbmpsm_check(self.h, C.byref(mass), mom)
+        if rc == ERR_NUMERIC:
+            raise LbmPsmError(rc, self.lib.lbmpsm_last_error(self.h).decode())
+        self._check(rc)
+        return mass.value, np.array(mom[:])
+
+    def stored_mask(self) -> np.ndarray:
+        """Nodes of the reference local array that the device stores (periodic halos excluded)."""
+        m = np.ones(self.local, dtype=bool)
+        dims = self.dimension
+        for d in range(dims):
+            if self.info.storage_dims[d] != self.local[d]:
+                idx = [slice(None)] * 3
+                idx[d] = 0
+                m[tuple(idx)] = False
+                idx[d] = self.local[d] - 1
+                m[tuple(idx)] = False
+        return m
