@@ -48,7 +48,8 @@ METRIC = "D3Q19 PSM MLUPS & % HBM roofline, FP32 vs FP64 at fixed drag error, 1 
 BYTES_PER_NODE = {"fp64": 2 * 19 * 8, "fp32": 2 * 19 * 4, "fp16": 2 * 19 * 2}
 
 
-def workload_params(edge=EDGE):
+def workload_params(edge=None):
+    edge = edge or EDGE
     lc = DIAM
     nu = (TAU - 0.5) / 3.0
     Re = U_WALL * lc / nu
@@ -58,8 +59,10 @@ def workload_params(edge=EDGE):
                 tau=TAU, Fext=(0.0, 0.0, 0.0))
 
 
-def rsa_spheres(edge=EDGE, n=NSPHERES, d=DIAM, seed=SEED):
+def rsa_spheres(edge=None, n=None, d=DIAM, seed=SEED):
     """Seeded random sequential addition, minimum image in the periodic x, z."""
+    edge = edge or EDGE
+    n = NSPHERES if n is None else n
     rng = np.random.default_rng(seed)
     L = np.array([edge, edge - 1.0, edge])
     r = d / 2
@@ -82,9 +85,10 @@ def rsa_spheres(edge=EDGE, n=NSPHERES, d=DIAM, seed=SEED):
     return acc, np.full(n, r)
 
 
-def images(edge=EDGE):
+def images(edge=None, nspheres=None):
     from lbmpsm.host import Domain, ghost_images
-    x, r = rsa_spheres(edge)
+    edge = edge or EDGE
+    x, r = rsa_spheres(edge, nspheres)
     n = len(x)
     prm = workload_params(edge)
     lo = prm["boxlo"]
@@ -178,10 +182,11 @@ def run_ours(args, rank=0, world=1):
 
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
-    g, nloc = images()
+    edge = args.edge
+    g, nloc = images(edge, args.nspheres)
     n = len(g.tag)
-    prm = workload_params()
-    nodes = EDGE * EDGE * EDGE
+    prm = workload_params(edge)
+    nodes = edge * edge * edge
 
     def make(storage):
         lat = lbmpsm.Lattice(**prm, storage=storage, device=device, max_images=n,
@@ -203,7 +208,7 @@ def run_ours(args, rank=0, world=1):
 
     K, W = args.steps, args.warmup
     # FP32 storage: the headline path
-    lat = make("fp32")
+    lat = make(args.storage)
     lat.step(g.tag, g.x, g.v, g.omega, g.radius)  # images go up once, map + step
     lat.apply_bc()
     lat.run_fixed(W)
@@ -233,22 +238,26 @@ def run_ours(args, rank=0, world=1):
     lat.close()
 
     # plain FP64 path on the same workload
-    lat64 = make("fp64")
-    lat64.step(g.tag, g.x, g.v, g.omega, g.radius)
-    lat64.apply_bc()
-    K64 = max(3, K // 4)
-    lat64.run_fixed(max(0, W + K - K64))  # same step count as the FP32 forces above
-    lat64.synchronize()
-    t64 = ev_time(lat64, lambda: lat64.run_fixed(K64))
-    f64_forces = lat64.read_forces(nloc)[0]
-    t64_kernel = ev_time(lat64, lattice_only(lat64, 3)) / 3
-    lat64.close()
+    fp64 = None
+    drag_err = None
+    if not args.no_fp64:
+        lat64 = make("fp64")
+        lat64.step(g.tag, g.x, g.v, g.omega, g.radius)
+        lat64.apply_bc()
+        K64 = max(3, K // 4)
+        lat64.run_fixed(max(0, W + K - K64))  # same step count as the FP32 forces above
+        lat64.synchronize()
+        t64 = ev_time(lat64, lambda: lat64.run_fixed(K64))
+        f64_forces = lat64.read_forces(nloc)[0]
+        t64_kernel = ev_time(lat64, lattice_only(lat64, 3)) / 3
+        lat64.close()
+        mlups64 = nodes * K64 / t64 / 1e6
+        drag_err = float(np.abs(f32_forces - f64_forces).max() / np.abs(f64_forces).max())
+        fp64 = (mlups64, t64_kernel)
 
     mlups = nodes * K * world / t_val / 1e6
-    mlups64 = nodes * K64 / t64 / 1e6
-    drag_err = float(np.abs(f32_forces - f64_forces).max() / np.abs(f64_forces).max())
     peak, peak_kind = measured_peak_gbs()
-    achieved = BYTES_PER_NODE["fp32"] * nodes / t_kernel / 1e9
+    achieved = BYTES_PER_NODE[args.storage] * nodes / t_kernel / 1e9
     traffic = profile_traffic()
     launches_per_step = 8  # map: prep, scan, fill, sort, apply; collide; reduce; bc
     out = {
@@ -262,12 +271,12 @@ def run_ours(args, rank=0, world=1):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32",  # FP32 collision arithmetic (FP32 or FP16 storage)
         "data": "synthetic",
         "config": {
-            "workload": "sheared suspension: D3Q19 256^3, y Zou-He shear walls +-0.01, tau 0.65, "
-                        "2000 spheres D=12 (seeded RSA, phi~0.108), FP32 storage, FP64 F/T/S",
-            "nodes": nodes, "particles": nloc, "images": n, "storage": "fp32",
+            "workload": f"sheared suspension: D3Q19 {edge}^3, y Zou-He shear walls +-0.01, tau 0.65, "
+                        f"{nloc} spheres D=12 (seeded RSA), {args.storage.upper()} storage, FP64 F/T/S",
+            "nodes": nodes, "particles": nloc, "images": n, "storage": args.storage,
             "l2": "lattice 1.27 GB > 129 MB L2: no flush needed",
             "parallelism": f"replicas x{world}",
         },
@@ -275,13 +284,13 @@ def run_ours(args, rank=0, world=1):
                 "h2d_bytes_per_step": int(n * (4 + 10 * 8)), "d2h_bytes_per_step": int(n * 12 * 8)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "collide_lowp_kernel<D3Q19,float> (A-A, even/odd)",
+                     "kernel": f"collide_lowp_kernel<D3Q19,{'float' if args.storage == 'fp32' else '__half'}> (A-A, even/odd)",
                      "algorithmic_bytes_per_node": BYTES_PER_NODE["fp32"],
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
-        "fp64_plain": {"value": round(mlups64, 1), "unit": "MLUPS",
-                       "kernel_ms": round(t64_kernel * 1e3, 3),
-                       "hbm_frac": round(BYTES_PER_NODE["fp64"] * nodes / t64_kernel / 1e9 / peak, 4)},
-        "fp32_over_fp64": round(mlups / world / mlups64, 2),
+        "fp64_plain": None if fp64 is None else {
+            "value": round(fp64[0], 1), "unit": "MLUPS", "kernel_ms": round(fp64[1] * 1e3, 3),
+            "hbm_frac": round(BYTES_PER_NODE["fp64"] * nodes / fp64[1] / 1e9 / peak, 4)},
+        "fp32_over_fp64": None if fp64 is None else round(mlups / world / fp64[0], 2),
         "drag_rel_err_fp32_vs_fp64": drag_err,
         "kernel_ms": round(t_kernel * 1e3, 4),
         "gpu_launches": launches_per_step * K,
@@ -356,6 +365,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--edge", type=int, default=EDGE, help="lattice edge (profiling cases)")
+    ap.add_argument("--nspheres", type=int, default=NSPHERES)
+    ap.add_argument("--storage", choices=["fp32", "fp16"], default="fp32")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))

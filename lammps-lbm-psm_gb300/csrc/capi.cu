@@ -53,7 +53,9 @@ struct lbmpsm_handle {
   Img* d_img = nullptr;
   int* d_cells = nullptr;   // count | off | fill (3*ncells)
   int* d_list = nullptr;
-  unsigned long long* d_pair_total = nullptr;
+  unsigned short* d_sfcode = nullptr;  // solid-fraction codes of (image, box node) pairs
+  long long sf_cap = 0;
+  unsigned long long* d_pair_total = nullptr;  // [0] list pairs, [1] codes
   int* d_status = nullptr;
   double* d_check = nullptr;
   void* h_stage = nullptr;  // pinned: inputs then outputs
@@ -216,6 +218,9 @@ void free_particles(lbmpsm_handle* h) {
   dfree(h->d_out);
   dfree(h->d_img);
   dfree(h->d_list);
+  dfree(h->d_sfcode);
+  h->d_sfcode = nullptr;
+  h->sf_cap = 0;
   h->d_tag = nullptr;
   h->d_xvw = nullptr;
   h->d_out = nullptr;
@@ -261,8 +266,10 @@ int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
     h->cap = cap;
     h->list_cap = 0;
   }
-  const double r_lb = max_r_phys / h->dx;
-  const long long need = (long long)std::max(n, 1) * cells_per_image(h, r_lb);
+  // size the cell lists for the full image capacity, so that *_device calls
+  // (which cannot grow buffers) never need more than was allocated
+  const double r_lb = std::max(max_r_phys, h->opt.max_radius) / h->dx;
+  const long long need = (long long)std::max(h->cap, 1) * cells_per_image(h, r_lb);
   if (need > h->list_cap) {
     drop_graphs(h);
     dfree(h->d_list);
@@ -270,6 +277,19 @@ int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
     long long cap = std::max(need, 2 * h->list_cap);
     CUDA_TRY(h, dmalloc(h, &h->d_list, sizeof(int) * (size_t)cap));
     h->list_cap = cap;
+  }
+  // solid-fraction codes: one per node of every image box, box edge <= 2r+6
+  const double edge = std::ceil(2.0 * r_lb + 6.0);
+  long long vol = 1;
+  for (int d = 0; d < h->g.dim; ++d) vol *= (long long)std::min<double>(edge, h->g.S[d]);
+  const long long need_sf = (long long)std::max(h->cap, 1) * vol;
+  if (need_sf > h->sf_cap) {
+    drop_graphs(h);
+    dfree(h->d_sfcode);
+    h->d_sfcode = nullptr;
+    long long cap = std::max(need_sf, 2 * h->sf_cap);
+    CUDA_TRY(h, dmalloc(h, &h->d_sfcode, sizeof(unsigned short) * (size_t)cap));
+    h->sf_cap = cap;
   }
   return LBMPSM_OK;
 }
@@ -292,6 +312,7 @@ int collide(lbmpsm_handle* h) {
   p.invCs2 = h->invCs2;
   p.invCs4 = h->invCs4;
   p.scale16 = h->scale16;
+  p.status = h->d_status;
   const int odd = (int)(h->t & 1);
   cudaError_t e;
   switch (h->opt.storage) {
@@ -319,7 +340,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
   if (n > 0) {
     const int ncells = h->C[0] * h->C[1] * h->C[2];
     CUDA_TRY(h, cudaMemsetAsync(h->d_cells, 0, sizeof(int) * 3 * (size_t)ncells, h->stream));
-    CUDA_TRY(h, cudaMemsetAsync(h->d_pair_total, 0, sizeof(unsigned long long), h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_pair_total, 0, 2 * sizeof(unsigned long long), h->stream));
     MapParams m{};
     m.g = h->g;
     m.tab = h->tab;
@@ -347,6 +368,8 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     m.list = h->d_list;
     m.list_cap = h->list_cap;
     m.pair_total = h->d_pair_total;
+    m.sfcode = h->d_sfcode;
+    m.sf_cap = h->sf_cap;
     m.status = h->d_status;
     m.write32 = h->opt.storage != LBMPSM_STORAGE_FP64 ? 1 : 0;
     CUDA_TRY(h, launch_map(m, h->stream));
@@ -398,6 +421,10 @@ int read_status(lbmpsm_handle* h) {
   int st = 0;
   CUDA_TRY(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (st & STATUS_TIMEOUT) {
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+    return fail(h, LBMPSM_ERR_TIMEOUT, "a bounded device-side wait on a bulk copy gave up");
+  }
   if (st & STATUS_LIST_OVERFLOW) {
     CUDA_TRY(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
     return fail(h, LBMPSM_ERR_CAPACITY,
@@ -512,7 +539,8 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
     g.off[d] = (real_axis && per) ? 1 : 0;
     g.S[d] = (real_axis && per) ? gn[d] : g.L[d];
   }
-  g.N = (long long)g.S[0] * g.S[1] * g.S[2];
+  g.P0 = (g.S[0] + 7) / 8 * 8;
+  g.N = (long long)g.P0 * g.S[1] * g.S[2];
   g.Np = (g.N + 63) / 64 * 64;
   h->cb[0] = 8;
   h->cb[1] = 8;
@@ -540,7 +568,7 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
     return bail(LBMPSM_ERR_NOMEM);
   const int ncells = h->C[0] * h->C[1] * h->C[2];
   if (dmalloc(h, &h->d_cells, sizeof(int) * 3 * (size_t)ncells) != cudaSuccess ||
-      dmalloc(h, &h->d_pair_total, sizeof(unsigned long long)) != cudaSuccess ||
+      dmalloc(h, &h->d_pair_total, 2 * sizeof(unsigned long long)) != cudaSuccess ||
       dmalloc(h, &h->d_status, sizeof(int)) != cudaSuccess ||
       dmalloc(h, &h->d_check, sizeof(double) * (4 + 4 * 1024)) != cudaSuccess)
     return bail(LBMPSM_ERR_NOMEM);

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
   if (sx >= g.S[0]) return;
   const int sy = row % g.S[1];
   const int sz = row / g.S[1];
-  const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
+  const long long n = node_index(g, sx, sy, sz);
   const Nbr nb = make_nbr(g, sx, sy, sz);
   double* __restrict__ F = static_cast<double*>(p.f);
   const long long Np = g.Np;
@@ -434,7 +434,7 @@ __global__ void bc_f64_kernel(BCParams p) {
     if (face_contains(p.face[k], sx, sy, sz)) return;
   const Geom& g = p.g;
   const Nbr nb = make_nbr(g, sx, sy, sz);
-  const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
+  const long long n = node_index(g, sx, sy, sz);
   double* F = static_cast<double*>(p.f);
   double f[Q];
   long long loc[Q];

@@ -116,35 +116,12 @@ struct UnrollF<L, L::Q> {
                                              bool, PsmNodeF&) {}
 };
 
-template <class L, typename T, bool ODD>
-__global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
+// Collision of one node on its 19 (or 9) deviations f[], in place: macro
+// values, optional macro store, PSM solid operator with node forces, Guo term.
+template <class L>
+__device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const CollideParams& p,
+                                                  long long n) {
   constexpr int Q = L::Q;
-  const Geom& g = p.g;
-  // blocks: (row, x-chunk) folded into blockIdx.x (rows can exceed the 65535 limit of y)
-  const int xblocks = (g.S[0] + blockDim.x - 1) / blockDim.x;
-  const int row = blockIdx.x / xblocks;
-  const int sx = (blockIdx.x - row * xblocks) * blockDim.x + threadIdx.x;
-  if (sx >= g.S[0]) return;
-  const int sy = row % g.S[1];
-  const int sz = row / g.S[1];
-  const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
-  const Nbr nb = make_nbr(g, sx, sy, sz);
-  T* __restrict__ F = static_cast<T*>(p.f);
-  const long long Np = g.Np;
-  const float sc = p.scale16;
-
-  float f[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
-    const bool ok = nbr_ok(nb, -cx, -cy, -cz);
-    if (!ODD) {
-      f[q] = ok ? Store<T>::load(F + q * Np + n, sc) : 0.0f;
-    } else {
-      const int o = nbr_off(nb, -cx, -cy, -cz);
-      f[q] = ok ? Store<T>::load(F + L::opp(q) * Np + n + o, sc) : 0.0f;
-    }
-  }
   float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -222,6 +199,39 @@ __global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
       nf[3 + c] = sn.F2[c];
     }
   }
+}
+
+// Direct variant: each thread gathers its node's populations from global
+// memory (used when an x-row is longer than one staged block).
+template <class L, typename T, bool ODD>
+__global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
+  constexpr int Q = L::Q;
+  const Geom& g = p.g;
+  // blocks: (row, x-chunk) folded into blockIdx.x (rows can exceed the 65535 limit of y)
+  const int xblocks = (g.S[0] + blockDim.x - 1) / blockDim.x;
+  const int row = blockIdx.x / xblocks;
+  const int sx = (blockIdx.x - row * xblocks) * blockDim.x + threadIdx.x;
+  if (sx >= g.S[0]) return;
+  const int sy = row % g.S[1];
+  const int sz = row / g.S[1];
+  const long long n = node_index(g, sx, sy, sz);
+  const Nbr nb = make_nbr(g, sx, sy, sz);
+  T* __restrict__ F = static_cast<T*>(p.f);
+  const long long Np = g.Np;
+  const float sc = p.scale16;
+  float f[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
+    const bool ok = nbr_ok(nb, -cx, -cy, -cz);
+    if (!ODD) {
+      f[q] = ok ? Store<T>::load(F + q * Np + n, sc) : 0.0f;
+    } else {
+      const int o = nbr_off(nb, -cx, -cy, -cz);
+      f[q] = ok ? Store<T>::load(F + L::opp(q) * Np + n + o, sc) : 0.0f;
+    }
+  }
+  collide_node_lowp<L>(f, p, n);
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
@@ -233,8 +243,225 @@ __global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
   }
 }
 
+// ------------------------------------------------------------- row staging
+// Bulk asynchronous copies (cp.async.bulk, the 1-D form of the tensor memory
+// accelerator path) between global memory and shared memory, completed on an
+// mbarrier for loads and through a bulk group for stores.
+__device__ __forceinline__ unsigned smem_addr(const void* ptr) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(ptr));
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred P1;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, P1;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(unsigned dst, const void* src, unsigned bytes,
+                                          unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* dst, unsigned src, unsigned bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+constexpr int STAGED_MAX_ROW = 256;      // nodes per x-row handled by one staged block
+constexpr long long MBAR_SPIN_LIMIT = 1ll << 26;
+
+// neighbour row (dy, dz) of row (sy, sz); false when it does not exist
+__device__ __forceinline__ bool row_of(const Geom& g, int sy, int sz, int dy, int dz,
+                                       long long& base) {
+  int y = sy + dy, z = sz + dz;
+  if (y < 0 || y >= g.S[1]) {
+    if (!g.per[1]) return false;
+    y = y < 0 ? y + g.S[1] : y - g.S[1];
+  }
+  if (z < 0 || z >= g.S[2]) {
+    if (!g.per[2]) return false;
+    z = z < 0 ? z + g.S[2] : z - g.S[2];
+  }
+  base = ((long long)z * g.S[1] + y) * g.P0;
+  return true;
+}
+
+// bit (dy+1)*3 + (dz+1) set when row (sy+dy, sz+dz) exists
+__device__ __forceinline__ unsigned row_mask(const Geom& g, int sy, int sz) {
+  unsigned m = 0;
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int y = sy + dy, z = sz + dz;
+      const bool oky = (y >= 0 && y < g.S[1]) || g.per[1];
+      const bool okz = (z >= 0 && z < g.S[2]) || g.per[2];
+      if (oky && okz) m |= 1u << ((dy + 1) * 3 + (dz + 1));
+    }
+  return m;
+}
+__host__ __device__ constexpr int row_bit(int dy, int dz) { return (dy + 1) * 3 + (dz + 1); }
+
+// Staged variant: one block per x-row (sy, sz), one thread per node.  The Q
+// population rows the step reads are pulled into shared memory with one bulk
+// copy each, the x-shifts of streaming are applied as shared-memory index
+// offsets, and the Q output rows are pushed back with one bulk copy each.
+//   even step: own row, slot q in, slot opp(q) out;
+//   odd step : row -e_q, slot opp(q) in -> row +e_q, slot q out.
+// The A-A pattern makes each block the only reader and writer of the
+// locations it moves, so blocks need no synchronisation between them.
+template <class L, typename T, bool ODD, bool FORCE>
+__global__ void __launch_bounds__(STAGED_MAX_ROW, 4) collide_staged_kernel(CollideParams p) {
+  constexpr int Q = L::Q;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const Geom& g = p.g;
+  const int P0 = g.P0;
+  T* buf = reinterpret_cast<T*>(smem_raw);
+  const unsigned bar = smem_addr(smem_raw + (size_t)Q * P0 * sizeof(T));
+  const unsigned row_bytes = (unsigned)(P0 * sizeof(T));
+  const int row = blockIdx.x;
+  const int sy = row % g.S[1];
+  const int sz = row / g.S[1];
+  const long long own = (long long)row * P0;
+  T* __restrict__ F = static_cast<T*>(p.f);
+  const long long Np = g.Np;
+  const float sc = p.scale16;
+  const unsigned rows = row_mask(g, sy, sz);
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned bytes = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+      if (!ODD || ((rows >> row_bit(-L::ey(q), -L::ez(q))) & 1u)) bytes += row_bytes;
+    mbar_expect_tx(bar, bytes);
+    long long base;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      if (!ODD) {
+        bulk_load(smem_addr(buf + q * P0), F + q * Np + own, row_bytes, bar);
+      } else if (row_of(g, sy, sz, -L::ey(q), -L::ez(q), base)) {
+        bulk_load(smem_addr(buf + q * P0), F + L::opp(q) * Np + base, row_bytes, bar);
+      }
+    }
+  }
+  // x neighbours of this thread's node (periodic wrap inside the row)
+  const int x = threadIdx.x;
+  const int S0 = g.S[0];
+  const bool active = x < S0;
+  const int xm = x > 0 ? x - 1 : S0 - 1;
+  const int xp = x < S0 - 1 ? x + 1 : 0;
+  const bool vxm = x > 0 || g.per[0];
+  const bool vxp = x < S0 - 1 || g.per[0];
+
+  bool ready = false;
+  for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it)
+    if (mbar_try_wait(bar, 0)) {
+      ready = true;
+      break;
+    }
+  if (!ready) {
+    if (threadIdx.x == 0) atomicOr(p.status, STATUS_TIMEOUT);
+    // let the copies already issued land before the block gives up its shared memory
+    for (long long it = 0; it < MBAR_SPIN_LIMIT && !mbar_try_wait(bar, 0); ++it) {
+    }
+    return;
+  }
+
+  float f[Q];
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      constexpr int dummy = 0;
+      (void)dummy;
+      const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
+      // the source node x - e_q exists: row and x neighbour
+      const bool ok = ((rows >> row_bit(-cy, -cz)) & 1u) && (cx == 0 || (cx > 0 ? vxm : vxp));
+      const int xs = ODD ? (cx == 0 ? x : (cx > 0 ? xm : xp)) : x;
+      f[q] = ok ? Store<T>::load(buf + q * P0 + xs, sc) : 0.0f;
+    }
+    CollideParams pp = p;
+    pp.has_force = FORCE ? 1 : 0;
+    collide_node_lowp<L>(f, pp, own + x);
+  }
+  __syncthreads();  // every input read before any output overwrites the rows
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      if (!ODD) {
+        Store<T>::store(buf + L::opp(q) * P0 + x, f[q], sc);
+      } else {
+        const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
+        const bool ok = ((rows >> row_bit(cy, cz)) & 1u) && (cx == 0 || (cx > 0 ? vxp : vxm));
+        const int xt = cx == 0 ? x : (cx > 0 ? xp : xm);
+        if (ok) Store<T>::store(buf + q * P0 + xt, f[q], sc);
+      }
+    }
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long base;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      if (!ODD) {
+        bulk_store(F + q * Np + own, smem_addr(buf + q * P0), row_bytes);
+      } else if (row_of(g, sy, sz, L::ey(q), L::ez(q), base)) {
+        bulk_store(F + q * Np + base, smem_addr(buf + q * P0), row_bytes);
+      }
+    }
+    bulk_commit();
+    bulk_wait_all();
+  }
+}
+
 template <class L, typename T>
 static cudaError_t launch_lowp(const CollideParams& p, int odd, cudaStream_t st) {
+  if (p.g.S[0] <= STAGED_MAX_ROW) {
+    const unsigned threads = (unsigned)((p.g.S[0] + 31) / 32 * 32);
+    const size_t smem = (size_t)L::Q * p.g.P0 * sizeof(T) + 16;
+    const unsigned rows = (unsigned)((long long)p.g.S[1] * p.g.S[2]);
+    if (odd) {
+      if (p.has_force)
+        collide_staged_kernel<L, T, true, true><<<rows, threads, smem, st>>>(p);
+      else
+        collide_staged_kernel<L, T, true, false><<<rows, threads, smem, st>>>(p);
+    } else {
+      if (p.has_force)
+        collide_staged_kernel<L, T, false, true><<<rows, threads, smem, st>>>(p);
+      else
+        collide_staged_kernel<L, T, false, false><<<rows, threads, smem, st>>>(p);
+    }
+    return cudaGetLastError();
+  }
   dim3 block(128);
   dim3 grid((unsigned)(((p.g.S[0] + block.x - 1) / block.x) * (long long)p.g.S[1] * p.g.S[2]));
   if (odd)
@@ -407,7 +634,7 @@ __global__ void bc_lowp_kernel(BCParams p) {
     if (face_has(p.face[k], sx, sy, sz)) return;
   const Geom& g = p.g;
   const Nbr nb = make_nbr(g, sx, sy, sz);
-  const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
+  const long long n = node_index(g, sx, sy, sz);
   T* F = static_cast<T*>(p.f);
   float f[Q];
   long long loc[Q];

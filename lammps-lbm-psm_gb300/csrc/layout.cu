@@ -90,7 +90,7 @@ __global__ void get_pop_kernel(Geom g, const void* f, int storage, int after_odd
       s[d] = h[d];
     }
   }
-  const long long n = ((long long)s[2] * g.S[1] + s[1]) * g.S[0] + s[0];
+  const long long n = node_index(g, s[0], s[1], s[2]);
   const Nbr nb = make_nbr(g, s[0], s[1], s[2]);
   for (int q = 0; q < L::Q; ++q) {
     const long long loc = loc_of<L>(g, nb, n, q, after_odd);
@@ -103,9 +103,10 @@ __global__ void set_pop_kernel(Geom g, void* f, int storage, int after_odd, floa
                                const double* in) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= g.N) return;
-  const int sx = (int)(n % g.S[0]);
-  const int sy = (int)((n / g.S[0]) % g.S[1]);
-  const int sz = (int)(n / ((long long)g.S[0] * g.S[1]));
+  const int sx = (int)(n % g.P0);
+  const int sy = (int)((n / g.P0) % g.S[1]);
+  const int sz = (int)(n / ((long long)g.P0 * g.S[1]));
+  if (sx >= g.S[0]) return;  // x padding
   const long long r = ((long long)(sx + g.off[0]) * g.L[1] + (sy + g.off[1])) * g.L[2] + (sz + g.off[2]);
   const Nbr nb = make_nbr(g, sx, sy, sz);
   for (int q = 0; q < L::Q; ++q) {
@@ -146,9 +147,10 @@ __global__ void check_partial_kernel(Geom g, const void* f, int storage, int aft
   bool bad = false;
   for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N;
        n += (long long)gridDim.x * blockDim.x) {
-    const int sx = (int)(n % g.S[0]);
-    const int sy = (int)((n / g.S[0]) % g.S[1]);
-    const int sz = (int)(n / ((long long)g.S[0] * g.S[1]));
+    const int sx = (int)(n % g.P0);
+    const int sy = (int)((n / g.P0) % g.S[1]);
+    const int sz = (int)(n / ((long long)g.P0 * g.S[1]));
+    if (sx >= g.S[0]) continue;  // x padding
     const Nbr nb = make_nbr(g, sx, sy, sz);
     for (int q = 0; q < L::Q; ++q) {
       const long long loc = loc_of<L>(g, nb, n, q, after_odd);

@@ -1,7 +1,8 @@
 // lbmpsm_internal.cuh -- shared definitions of the GB300 LBM-PSM library.
 //
 // Device data layout (one lattice = one handle):
-//   populations  SoA, f[q*Np + node], node = (sz*S1 + sy)*S0 + sx, x fastest.
+//   populations  SoA, f[q*Np + node], node = (sz*S1 + sy)*P0 + sx, x fastest,
+//                rows padded to a pitch P0 that is a multiple of 8.
 //                In-place "A-A" streaming: even steps read and write a node's
 //                own slots (writing direction q into slot opp(q)), odd steps
 //                gather from and scatter to the neighbours.  One copy of the
@@ -77,9 +78,14 @@ struct Geom {
   int S[3];    // device storage extents
   int off[3];  // reference index h = s + off
   int per[3];  // periodic axes wrap; the 2-D z axis counts as periodic
-  long long N; // S0*S1*S2
+  int P0;      // x pitch: S0 rounded up to 8 so that every x-row starts 16-byte aligned
+  long long N; // P0*S1*S2 (node slots including the x padding)
   long long Np;// population stride (N rounded up to 64)
 };
+
+__host__ __device__ __forceinline__ long long node_index(const Geom& g, int sx, int sy, int sz) {
+  return ((long long)sz * g.S[1] + sy) * g.P0 + sx;
+}
 
 // Neighbour offsets of one node: o[axis][0] towards -1, o[axis][1] towards +1
 // (in nodes); v bit (2*axis + side) set when that neighbour exists.
@@ -92,7 +98,7 @@ __device__ __forceinline__ Nbr make_nbr(const Geom& g, int sx, int sy, int sz) {
   Nbr nb;
   nb.v = 0;
   const int s[3] = {sx, sy, sz};
-  const int stride[3] = {1, g.S[0], g.S[0] * g.S[1]};
+  const int stride[3] = {1, g.P0, g.P0 * g.S[1]};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const int n = g.S[a];
@@ -160,6 +166,7 @@ struct CollideParams {
   int has_force;          // |F_lbm|^2 > 0
   double invCs2, invCs4;
   float scale16;          // FP16 storage: stored value = deviation * scale16
+  int* status;            // error word (STATUS_*)
 };
 
 // Zou-He face list of one `fix lbm-psm-bc` keyword.
@@ -194,7 +201,20 @@ struct Img {
   double r;           // radius, lattice units
   double uT[3];       // translational velocity, lattice units
   double om[3];       // angular velocity, lattice units
+  // exact FP64 thresholds of calcSolidFraction (r+h)^2, (r-h)^2, r^2
+  double rP2, rM2, rSq;
+  // FP32 helpers: xl = xi + xfrac exactly; node offset dx = (h - xi) - xfrac
+  int xi[3];
+  float xf[3];
+  float rP2f, rM2f, rSqf;
+  int has_spin;       // any omega component non-zero
+  long long sf_off;   // offset of this image's box in the solid-fraction code scratch
+  int box[3];         // box extents (hi - lo)
 };
+
+// Solid-fraction codes of one (image, node) pair: 0..1000 = number of
+// sub-cell centres inside (sf = n/10^d), SF_ONE = the early-out value 1.0.
+constexpr unsigned short SF_ONE = 0xFFFF;
 
 struct MapParams {
   Geom g;
@@ -216,7 +236,9 @@ struct MapParams {
   int* cell_fill;
   int* list;
   long long list_cap;
-  unsigned long long* pair_total;
+  unsigned long long* pair_total;  // [0] cell-list pairs, [1] solid-fraction codes
+  unsigned short* sfcode;          // codes of all (image, box node) pairs
+  long long sf_cap;
   int* status;
   int write32;        // also write the FP32 mirror
 };
@@ -238,7 +260,7 @@ struct ReduceParams {
 };
 
 // status bits
-enum : int { STATUS_LIST_OVERFLOW = 1, STATUS_NONFINITE = 2 };
+enum : int { STATUS_LIST_OVERFLOW = 1, STATUS_NONFINITE = 2, STATUS_TIMEOUT = 4 };
 
 // ---------------------------------------------------------------- launchers
 // collide.cu / collide_f32.cu

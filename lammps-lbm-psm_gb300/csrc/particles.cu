@@ -73,6 +73,38 @@ __global__ void img_prep_kernel(MapParams p) {
     im.om[d] = p.omega[3 * i + d] * p.tc * p.dt_d;
   }
   im.valid = valid;
+  {
+    const double rP = r + p.sqrt2half;
+    const double rM = r - p.sqrt2half;
+    im.rP2 = rP * rP;
+    im.rM2 = rM * rM;
+    im.rSq = r * r;
+    im.rP2f = (float)im.rP2;
+    im.rM2f = (float)im.rM2;
+    im.rSqf = (float)im.rSq;
+    for (int d = 0; d < 3; ++d) {
+      // xl = xi + xfrac exactly (the fractional part of a double is exact)
+      const double xl = im.xl[d];
+      const bool small = fabs(xl) < 1.0e9;
+      const double fl = small ? floor(xl) : 0.0;
+      im.xi[d] = (int)fl;
+      im.xf[d] = (float)(xl - fl);
+    }
+    // the node velocity reduces to uT + 0.0 bit for bit when every omega
+    // component is +0.0 and no uT component is -0.0 (signed-zero arithmetic)
+    bool plain = true;
+    for (int d = 0; d < 3; ++d) {
+      if (__double_as_longlong(im.om[d]) != 0ll) plain = false;
+      if (__double_as_longlong(im.uT[d]) == (long long)0x8000000000000000ull) plain = false;
+    }
+    im.has_spin = plain ? 0 : 1;
+  }
+  im.sf_off = 0;
+  for (int d = 0; d < 3; ++d) im.box[d] = valid ? im.hi[d] - im.lo[d] : 0;
+  if (valid) {
+    const unsigned long long vol = (unsigned long long)im.box[0] * im.box[1] * im.box[2];
+    im.sf_off = (long long)atomicAdd(&p.pair_total[1], vol);
+  }
   long long ncell = 0;
   if (valid) {
     for (int d = 0; d < 3; ++d) {
@@ -85,7 +117,7 @@ __global__ void img_prep_kernel(MapParams p) {
       for (int cy = im.clo[1]; cy <= im.chi[1]; ++cy)
         for (int cx = im.clo[0]; cx <= im.chi[0]; ++cx)
           atomicAdd(&p.cell_count[(cz * p.C[1] + cy) * p.C[0] + cx], 1);
-    atomicAdd(p.pair_total, (unsigned long long)ncell);
+    atomicAdd(&p.pair_total[0], (unsigned long long)ncell);
   } else {
     for (int d = 0; d < 3; ++d) im.clo[d] = 0, im.chi[d] = -1;
   }
@@ -119,7 +151,8 @@ __global__ void cell_scan_kernel(const int* __restrict__ count, int* __restrict_
 __global__ void img_fill_kernel(MapParams p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
-  if (*p.pair_total > (unsigned long long)p.list_cap) {
+  if (p.pair_total[0] > (unsigned long long)p.list_cap ||
+      p.pair_total[1] > (unsigned long long)p.sf_cap) {
     if (i == 0) atomicOr(p.status, STATUS_LIST_OVERFLOW);
     return;
   }
@@ -137,7 +170,7 @@ __global__ void img_fill_kernel(MapParams p) {
 __global__ void cell_sort_kernel(MapParams p, int ncells) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
-  if (*p.pair_total > (unsigned long long)p.list_cap) return;
+  if (p.pair_total[0] > (unsigned long long)p.list_cap) return;
   int* a = p.list + p.cell_off[c];
   const int m = p.cell_count[c];
   for (int k = 1; k < m; ++k) {
@@ -151,119 +184,238 @@ __global__ void cell_sort_kernel(MapParams p, int ncells) {
   }
 }
 
-// calcSolidFraction (src/LBM_PSM_exchangeParticleData.cpp:116-169)
-static __device__ double solid_fraction(int dim, int i, int j, int k, double xP, double yP,
-                                        double zP, double rP_LB, double sqrt2half) {
-  const int slicesPerDim = 10;
-  const double sliceWidth = 1.0 / ((double)slicesPerDim);
-  double fraction = 1.0 / ((double)(slicesPerDim * slicesPerDim));
-  if (dim == 3) fraction = 1.0 / ((double)(slicesPerDim * slicesPerDim * slicesPerDim));
-  const double dx = (double)i - xP;
-  const double dy = (double)j - yP;
-  const double dz = (double)k - zP;
-  const double dist = dx * dx + dy * dy + dz * dz;
-  const double rP = rP_LB + sqrt2half;
-  if (dist > rP * rP) return 0.0;
-  const double rM = rP_LB - sqrt2half;
-  if (dist < rM * rM) return 1.0;
-  const double rSq = rP_LB * rP_LB;
-  double ax[10], ay[10], az[10];
-  float fa[10], fb[10], fc[10];
-  float amax = 0.f, bmax = 0.f, cmax = 0.f;
-#pragma unroll
-  for (int m = 0; m < 10; ++m) {
-    const double delta = -0.5 + ((double)m + 0.5) * sliceWidth;
-    const double dxi = dx + delta;
-    ax[m] = dxi * dxi;
-    const double dyi = dy + delta;
-    ay[m] = dyi * dyi;
-    const double dzi = dz + delta;
-    az[m] = dzi * dzi;
-    fa[m] = (float)ax[m];
-    fb[m] = (float)ay[m];
-    fc[m] = (float)az[m];
-    amax = fmaxf(amax, fa[m]);
-    bmax = fmaxf(bmax, fb[m]);
-    cmax = fmaxf(cmax, fc[m]);
-  }
-  const float R = (float)rSq;
+// calcSolidFraction (src/LBM_PSM_exchangeParticleData.cpp:116-169): the
+// sub-cell count evaluated exactly in FP64 with the reference's expressions,
+// split over the 8 lanes of a group (lane `sub` takes the (a, b) rows sub,
+// sub+8, ...).  All 32 lanes of the warp must call it (shuffles); lanes of
+// groups without work pass valid = false.  Used whenever an FP32 decision
+// cannot be proven equal to the reference's.
+static __device__ int subcell_count_exact_group8(bool valid, int dim, double dx, double dy,
+                                                 double dz, double rP_LB, int sub) {
   int n = 0;
-  if (dim == 2) {
-    const float margin = 1.52587890625e-05f * fmaxf(R, amax + bmax);  // 2^-16
-    for (int a = 0; a < 10; ++a) {
+  if (valid) {
+    const double sliceWidth = 1.0 / ((double)10);
+    const double rSq = rP_LB * rP_LB;
+    double az[10];
 #pragma unroll
-      for (int b = 0; b < 10; ++b) {
-        const float d = (fa[a] + fb[b]) - R;
-        if (d < -margin)
-          ++n;
-        else if (d <= margin && ax[a] + ay[b] < rSq)
-          ++n;
+    for (int c = 0; c < 10; ++c) {
+      const double delta = -0.5 + ((double)c + 0.5) * sliceWidth;
+      const double dzi = dz + delta;
+      az[c] = dzi * dzi;
+    }
+    for (int r = sub; r < 100; r += 8) {
+      const int a = r / 10, b = r % 10;
+      const double da = dx + (-0.5 + ((double)a + 0.5) * sliceWidth);
+      const double db = dy + (-0.5 + ((double)b + 0.5) * sliceWidth);
+      const double ax = da * da, ay = db * db;
+      if (dim == 2) {
+        if (ax + ay < rSq) ++n;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 10; ++c)
+          if (ax + ay + az[c] < rSq) ++n;
       }
     }
-  } else {
-    const float margin = 1.52587890625e-05f * fmaxf(R, amax + bmax + cmax);
-    for (int a = 0; a < 10; ++a) {
-      for (int b = 0; b < 10; ++b) {
-        const float s = fa[a] + fb[b];
+  }
 #pragma unroll
-        for (int c = 0; c < 10; ++c) {
-          const float d = (s + fc[c]) - R;
-          if (d < -margin)
-            ++n;
-          else if (d <= margin && ax[a] + ay[b] + az[c] < rSq)
-            ++n;
+  for (int o = 4; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  return n;
+}
+
+// Early-out part of calcSolidFraction for one node, decided in FP32 with a
+// proven margin, else in FP64 with the reference's expressions.  Returns a
+// code (0 or SF_ONE) or -1 for a shell node whose sub-cells must be counted.
+//
+// Offsets dx = (double)h - xl are formed as (h - xi) - xfrac with xl = xi + xfrac
+// split exactly, so |dxf - dx| <= u(|dx| + 1), u = 2^-24, and the FP32 squared
+// distance obeys |d32 - dist| <= u(5 dist + 2 sum|d|).  The margin m is 16x that.
+static __device__ __forceinline__ int classify_node(int hi, int hj, int hk, const Img& im,
+                                                    float& dxf, float& dyf, float& dzf) {
+  const float u = 5.9604644775390625e-08f;  // 2^-24
+  dxf = (float)(hi - im.xi[0]) - im.xf[0];
+  dyf = (float)(hj - im.xi[1]) - im.xf[1];
+  dzf = (float)(hk - im.xi[2]) - im.xf[2];
+  const float d32 = dxf * dxf + dyf * dyf + dzf * dzf;
+  const float ad = fabsf(dxf) + fabsf(dyf) + fabsf(dzf);
+  const float m = 16.0f * u * (5.0f * d32 + 2.0f * ad + 1.0f + im.rP2f);
+  if (d32 > im.rP2f + m) return 0;
+  const bool nearP = d32 >= im.rP2f - m;
+  const bool nearM = d32 >= im.rM2f - m && d32 <= im.rM2f + m;
+  if (nearP || nearM) {
+    const double dx = (double)hi - im.xl[0];
+    const double dy = (double)hj - im.xl[1];
+    const double dz = (double)hk - im.xl[2];
+    const double dist = dx * dx + dy * dy + dz * dz;
+    if (dist > im.rP2) return 0;
+    if (dist < im.rM2) return SF_ONE;
+    return -1;
+  }
+  if (d32 < im.rM2f) return SF_ONE;  // below rM^2 - m: inside for certain
+  return -1;
+}
+
+// Sub-cell count of a shell node by an 8-lane group, in FP32 with a proven
+// margin.  The sub-cell sums A+B+C are formed with the innermost loop along the
+// axis most nearly tangent to the surface (smallest |d|), so that most rows
+// of 10 are entirely inside or outside and decided by one comparison with the
+// row's extreme (FP32 addition is monotone).  Per-term error |fa - A| <= 5u Ex^2
+// with Ex = |dx| + 2 (the FP32 sub-cell offsets are within 1.7u of the
+// reference's); sum error <= 7.1u Emax; margin 16u(Emax + r^2).  amb != 0 when
+// a sub-cell sum falls inside the margin (exact FP64 count needed).  All 32
+// lanes call it; lanes of groups without work pass valid = false.
+static __device__ void subcell_count_fast_group8(bool valid, int dim, float dxf, float dyf,
+                                                 float dzf, const Img& im, int sub, int& n_out,
+                                                 int& amb_out) {
+  const float u = 5.9604644775390625e-08f;
+  int n = 0, amb = 0;
+  if (valid) {
+    float da = dxf, db = dyf, dc = dzf;
+    if (dim == 3) {
+      const float ax = fabsf(dxf), ay = fabsf(dyf), az = fabsf(dzf);
+      if (ax <= ay && ax <= az) {
+        da = dyf; db = dzf; dc = dxf;
+      } else if (ay <= ax && ay <= az) {
+        da = dxf; db = dzf; dc = dyf;
+      }
+    }
+    const float Ea = fabsf(da) + 2.0f, Eb = fabsf(db) + 2.0f, Ec = fabsf(dc) + 2.0f;
+    const float R = im.rSqf;
+    // rows r = sub + 8k: (a, b) = (r / 10, r % 10), advanced incrementally
+    int a = sub / 10, b = sub % 10;
+    if (dim == 2) {
+      const float M = 16.0f * u * (Ea * Ea + Eb * Eb + R);
+      const float lo = R - M, hi = R + M;
+      for (int r = sub; r < 100; r += 8) {
+        const float ta = da + (-0.45f + 0.1f * (float)a);
+        const float tb = db + (-0.45f + 0.1f * (float)b);
+        const float t = ta * ta + tb * tb;
+        n += (t < lo);
+        amb += (t >= lo) & (t <= hi);
+        b += 8;
+        if (b >= 10) {
+          b -= 10;
+          ++a;
+        }
+      }
+    } else {
+      const float M = 16.0f * u * (Ea * Ea + Eb * Eb + Ec * Ec + R);
+      const float lo = R - M, hi = R + M;
+      float fc[10];
+      float cmin = 3.4e38f, cmax = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 10; ++c) {
+        const float tc = dc + (float)(-0.5 + ((double)c + 0.5) * 0.1);
+        fc[c] = tc * tc;
+        cmin = fminf(cmin, fc[c]);
+        cmax = fmaxf(cmax, fc[c]);
+      }
+      for (int r = sub; r < 100; r += 8) {
+        const float ta = da + (-0.45f + 0.1f * (float)a);
+        const float tb = db + (-0.45f + 0.1f * (float)b);
+        const float s = ta * ta + tb * tb;
+        if (s + cmax < lo) {
+          n += 10;
+        } else if (!(s + cmin > hi)) {
+#pragma unroll
+          for (int c = 0; c < 10; ++c) {
+            const float t = s + fc[c];
+            n += (t < lo);
+            amb += (t >= lo) & (t <= hi);
+          }
+        }
+        b += 8;
+        if (b >= 10) {
+          b -= 10;
+          ++a;
         }
       }
     }
   }
-  return fraction * ((double)n);
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) {
+    n += __shfl_xor_sync(0xffffffffu, n, o);
+    amb += __shfl_xor_sync(0xffffffffu, amb, o);
+  }
+  n_out = n;
+  amb_out = amb;
 }
 
-// setParticleOnLattice / setToZero on a register copy of one node's slots
-struct NodeSlots {
-  int id[2];
-  double eps[2];
-  double us[6];
-};
+constexpr int SF_THREADS = 256;
+constexpr int SF_ROUND = 2048;
 
-static __device__ __forceinline__ void set_particle(NodeSlots& s, int pID, const double* uP,
-                                                    double eps) {
-  int slot = -1;
-  if (s.id[0] == pID)
-    slot = 0;
-  else if (s.id[1] == pID)
-    slot = 1;
-  else if (pID != s.id[0] && pID != s.id[1] && s.id[0] == 0)
-    slot = 0;
-  else if (pID != s.id[0] && pID != s.id[1] && s.id[1] == 0)
-    slot = 1;
-  if (slot < 0) return;  // a third particle on the node is dropped
-  s.id[slot] = pID;
-  s.eps[slot] = eps;
-  s.us[3 * slot + 0] = uP[0];
-  s.us[3 * slot + 1] = uP[1];
-  s.us[3 * slot + 2] = uP[2];
+// Phase 1 of the map: solid-fraction codes of every node of every image box
+// (independent of image order).  One block per image; nodes are classified
+// by their threads, shell nodes queued in shared memory and counted by whole
+// warps.
+__global__ void __launch_bounds__(SF_THREADS) sf_kernel(MapParams p) {
+  const Img& im = p.img[blockIdx.x];
+  if (!im.valid) return;
+  if (p.pair_total[0] > (unsigned long long)p.list_cap ||
+      p.pair_total[1] > (unsigned long long)p.sf_cap)
+    return;
+  const Geom& g = p.g;
+  const int wx = im.box[0], wy = im.box[1], wz = im.box[2];
+  const int vol = wx * wy * wz;
+  unsigned short* code = p.sfcode + im.sf_off;
+  __shared__ int queue[SF_ROUND];
+  __shared__ int qn;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < vol; base += SF_ROUND) {
+    if (threadIdx.x == 0) qn = 0;
+    __syncthreads();
+    const int end = min(vol, base + SF_ROUND);
+    for (int li = base + threadIdx.x; li < end; li += SF_THREADS) {
+      const int sx = im.lo[0] + li % wx;
+      const int sy = im.lo[1] + (li / wx) % wy;
+      const int sz = im.lo[2] + li / (wx * wy);
+      float dxf, dyf, dzf;
+      const int c = classify_node(sx + g.off[0], sy + g.off[1], sz + g.off[2], im, dxf, dyf, dzf);
+      if (c >= 0)
+        code[li] = (unsigned short)c;
+      else
+        queue[atomicAdd(&qn, 1)] = li;
+    }
+    __syncthreads();
+    const int nq = qn;
+    // four shell nodes per warp, one 8-lane group each
+    const int grp = lane >> 3, sub = lane & 7;
+    for (int e0 = warp * 4; e0 < nq; e0 += (SF_THREADS / 32) * 4) {
+      const int e = e0 + grp;
+      const bool valid = e < nq;
+      const int li = valid ? queue[e] : 0;
+      const int hi = im.lo[0] + li % wx + g.off[0];
+      const int hj = im.lo[1] + (li / wx) % wy + g.off[1];
+      const int hk = im.lo[2] + li / (wx * wy) + g.off[2];
+      const float dxf = (float)(hi - im.xi[0]) - im.xf[0];
+      const float dyf = (float)(hj - im.xi[1]) - im.xf[1];
+      const float dzf = (float)(hk - im.xi[2]) - im.xf[2];
+      int nc, amb;
+      subcell_count_fast_group8(valid, g.dim, dxf, dyf, dzf, im, sub, nc, amb);
+      const bool need_exact = valid && amb != 0;
+      if (__any_sync(0xffffffffu, need_exact)) {
+        const int ne = subcell_count_exact_group8(need_exact, g.dim, (double)hi - im.xl[0],
+                                                  (double)hj - im.xl[1], (double)hk - im.xl[2],
+                                                  im.r, sub);
+        if (need_exact) nc = ne;
+      }
+      if (valid && sub == 0) code[li] = (unsigned short)nc;
+    }
+    __syncthreads();
+  }
 }
 
-static __device__ __forceinline__ void set_to_zero(NodeSlots& s, int pID) {
-  int slot = -1;
-  if (s.id[0] == pID)
-    slot = 0;
-  else if (s.id[1] == pID)
-    slot = 1;
-  if (slot < 0) return;
-  s.id[slot] = 0;
-  s.eps[slot] = 0.0;
-  s.us[3 * slot + 0] = 0.0;
-  s.us[3 * slot + 1] = 0.0;
-  s.us[3 * slot + 2] = 0.0;
-}
-
-__global__ void node_apply_kernel(MapParams p) {
+// Phase 2 of the map: per node, the images whose boxes contain it, in image
+// order, through the 4-way update of setParticlesOnLattice
+// (src/LBM_PSM_exchangeParticleData.cpp:69-106) on the two-slot table
+// (setParticleOnLattice / setToZero, src/LBM_PSM_lattice.cpp:257-324).
+// The table is written back only where it changed.
+__global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
   const int c = blockIdx.x;
   const int cnt = p.cell_count[c];
   if (cnt == 0) return;
-  if (*p.pair_total > (unsigned long long)p.list_cap) return;
+  if (p.pair_total[0] > (unsigned long long)p.list_cap ||
+      p.pair_total[1] > (unsigned long long)p.sf_cap)
+    return;
   const Geom& g = p.g;
   const int cx = c % p.C[0];
   const int cy = (c / p.C[0]) % p.C[1];
@@ -272,70 +424,123 @@ __global__ void node_apply_kernel(MapParams p) {
   const int sy = cy * p.cb[1] + threadIdx.y;
   const int sz = cz * p.cb[2] + threadIdx.z;
   if (sx >= g.S[0] || sy >= g.S[1] || sz >= g.S[2]) return;
-  const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
+  const long long n = node_index(g, sx, sy, sz);
   const int hi = sx + g.off[0], hj = sy + g.off[1], hk = sz + g.off[2];
+  const double fraction = g.dim == 3 ? 1.0 / ((double)(10 * 10 * 10)) : 1.0 / ((double)(10 * 10));
   const int* lst = p.list + p.cell_off[c];
-  NodeSlots s;
-  bool loaded = false;
+  int id[2] = {0, 0};
+  double eps[2] = {0.0, 0.0};
+  bool have_ids = false, have_eps = false, ids_dirty = false;
+  bool slot_dirty[2] = {false, false};
+  double us[6];
   for (int t = 0; t < cnt; ++t) {
     const Img& im = p.img[lst[t]];
     if (sx < im.lo[0] || sx >= im.hi[0] || sy < im.lo[1] || sy >= im.hi[1] || sz < im.lo[2] ||
         sz >= im.hi[2])
       continue;
-    if (!loaded) {
-      const int2 id = p.tab.ids[n];
-      const double2 e = p.tab.eps[n];
-      s.id[0] = id.x;
-      s.id[1] = id.y;
-      s.eps[0] = e.x;
-      s.eps[1] = e.y;
-      for (int k = 0; k < 6; ++k) s.us[k] = p.tab.us[6 * n + k];
-      loaded = true;
+    if (!have_ids) {
+      const int2 v = p.tab.ids[n];
+      id[0] = v.x;
+      id[1] = v.y;
+      have_ids = true;
     }
     const int tag = im.tag;
-    const double sf = solid_fraction(g.dim, hi, hj, hk, im.xl[0], im.xl[1], im.xl[2], im.r,
-                                     p.sqrt2half);
-    int id_old = 0;
-    double sf_old = 0.0;
-    if (tag == s.id[0]) {
-      id_old = s.id[0];
-      sf_old = s.eps[0];
-    } else if (tag == s.id[1]) {
-      id_old = s.id[1];
-      sf_old = s.eps[1];
+    const int li = ((sz - im.lo[2]) * im.box[1] + (sy - im.lo[1])) * im.box[0] + (sx - im.lo[0]);
+    const unsigned short cd = p.sfcode[im.sf_off + li];
+    // sf = n/10^d (or the early-out 1.0) exceeds 1e-5 exactly when n > 0
+    const bool sf_pos = cd != 0;
+    const int match = tag == id[0] ? 0 : (tag == id[1] ? 1 : -1);
+    bool old_pos = false;
+    if (match >= 0) {
+      if (!have_eps) {
+        const double2 e = p.tab.eps[n];
+        eps[0] = e.x;
+        eps[1] = e.y;
+        have_eps = true;
+      }
+      old_pos = eps[match] > 0.00001;
     }
-    const int decFlag = (sf > 0.00001) + 2 * (sf_old > 0.00001);
-    const double dx = (double)hi - im.xl[0];
-    const double dy = (double)hj - im.xl[1];
-    const double dz = (double)hk - im.xl[2];
-    double uNode[3];
-    uNode[0] = im.uT[0] + im.om[1] * dz - im.om[2] * dy;
-    uNode[1] = im.uT[1] + im.om[2] * dx - im.om[0] * dz;
-    uNode[2] = im.uT[2] + im.om[0] * dy - im.om[1] * dx;
+    // decFlag = (sf > 1e-5) + 2*(sf_old > 1e-5); sf_old > 1e-5 implies the tag
+    // holds a slot (id_old == tag), which makes case 3 always set and case 2
+    // always clear
+    const int decFlag = (sf_pos ? 1 : 0) + (old_pos ? 2 : 0);
+    int set = -2;  // -2: nothing, -1: clear the tag, 0: set
     switch (decFlag) {
       case 0:
-        set_to_zero(s, tag);
+        set = -1;
         break;
       case 1:
-        set_particle(s, tag, uNode, sf);
+        set = 0;
         break;
       case 2:
-        if (id_old == tag) set_to_zero(s, tag);
+        set = -1;
         break;
       case 3:
-        if (sf > sf_old || id_old == tag) set_particle(s, tag, uNode, sf);
+        set = 0;
         break;
     }
+    if (set == -1 && match >= 0) {  // setToZero
+      if (!have_eps) {
+        const double2 e = p.tab.eps[n];
+        eps[0] = e.x;
+        eps[1] = e.y;
+        have_eps = true;
+      }
+      id[match] = 0;
+      eps[match] = 0.0;
+      us[3 * match] = us[3 * match + 1] = us[3 * match + 2] = 0.0;
+      ids_dirty = true;
+      slot_dirty[match] = true;
+    } else if (set == 0) {  // setParticleOnLattice: matching slot, else first empty, else drop
+      int slot = -1;
+      if (id[0] == tag)
+        slot = 0;
+      else if (id[1] == tag)
+        slot = 1;
+      else if (id[0] == 0)
+        slot = 0;
+      else if (id[1] == 0)
+        slot = 1;
+      if (slot >= 0) {
+        if (!have_eps) {
+          const double2 e = p.tab.eps[n];
+          eps[0] = e.x;
+          eps[1] = e.y;
+          have_eps = true;
+        }
+        if (id[slot] != tag) ids_dirty = true;
+        id[slot] = tag;
+        eps[slot] = cd == SF_ONE ? 1.0 : fraction * ((double)cd);
+        // rigid-body velocity of the node (src/LBM_PSM_exchangeParticleData.cpp:83-89)
+        if (im.has_spin) {
+          const double dx = (double)hi - im.xl[0];
+          const double dy = (double)hj - im.xl[1];
+          const double dz = (double)hk - im.xl[2];
+          us[3 * slot + 0] = im.uT[0] + im.om[1] * dz - im.om[2] * dy;
+          us[3 * slot + 1] = im.uT[1] + im.om[2] * dx - im.om[0] * dz;
+          us[3 * slot + 2] = im.uT[2] + im.om[0] * dy - im.om[1] * dx;
+        } else {
+          // with omega == 0 the cross-product terms are signed zeros: the
+          // reference's (uT + 0*dz) - 0*dy equals uT + 0.0 bit for bit
+          us[3 * slot + 0] = im.uT[0] + 0.0;
+          us[3 * slot + 1] = im.uT[1] + 0.0;
+          us[3 * slot + 2] = im.uT[2] + 0.0;
+        }
+        slot_dirty[slot] = true;
+      }
+    }
   }
-  if (!loaded) return;
-  p.tab.ids[n] = make_int2(s.id[0], s.id[1]);
-  p.tab.eps[n] = make_double2(s.eps[0], s.eps[1]);
-  for (int k = 0; k < 6; ++k) p.tab.us[6 * n + k] = s.us[k];
-  p.tab.flag[n] = (uint8_t)((s.id[0] > 0 ? 1 : 0) | (s.id[1] > 0 ? 2 : 0));
-  if (p.write32) {
-    p.tab.rec32[2 * n] = make_float4((float)s.eps[0], (float)s.us[0], (float)s.us[1], (float)s.us[2]);
-    p.tab.rec32[2 * n + 1] =
-        make_float4((float)s.eps[1], (float)s.us[3], (float)s.us[4], (float)s.us[5]);
+  if (ids_dirty) {
+    p.tab.ids[n] = make_int2(id[0], id[1]);
+    p.tab.flag[n] = (uint8_t)((id[0] > 0 ? 1 : 0) | (id[1] > 0 ? 2 : 0));
+  }
+  if (slot_dirty[0] || slot_dirty[1]) p.tab.eps[n] = make_double2(eps[0], eps[1]);
+  for (int b = 0; b < 2; ++b) {
+    if (!slot_dirty[b]) continue;
+    for (int k = 0; k < 3; ++k) p.tab.us[6 * n + 3 * b + k] = us[3 * b + k];
+    if (p.write32)
+      p.tab.rec32[2 * n + b] = make_float4((float)eps[b], (float)us[3 * b], (float)us[3 * b + 1],
+                                           (float)us[3 * b + 2]);
   }
 }
 
@@ -347,6 +552,7 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   cell_scan_kernel<<<1, 1024, 0, st>>>(p.cell_count, p.cell_off, ncells);
   img_fill_kernel<<<(p.n + tb - 1) / tb, tb, 0, st>>>(p);
   cell_sort_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(p, ncells);
+  sf_kernel<<<p.n, SF_THREADS, 0, st>>>(p);
   dim3 block(p.cb[0], p.cb[1], p.cb[2]);
   node_apply_kernel<<<ncells, block, 0, st>>>(p);
   return cudaGetLastError();
@@ -355,86 +561,44 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
 // ------------------------------------------------------------------ reduce
 constexpr int RED_THREADS = 256;
 
-__global__ void __launch_bounds__(RED_THREADS) reduce_kernel(ReduceParams p) {
-  const int ip = blockIdx.x;
-  const Geom& g = p.g;
-  const int tag = p.tag[ip];
-  const double r = p.radius[ip] / p.dx;
+// Box of one image clamped to interior nodes (src/LBM_PSM_exchangeParticleData.cpp:188-195).
+struct RedBox {
   double xl[3];
   int lo[3], hi[3];
+};
+
+static __device__ __forceinline__ RedBox reduce_box(const ReduceParams& p, int ip) {
+  const Geom& g = p.g;
+  RedBox b;
+  const double r = p.radius[ip] / p.dx;
   for (int d = 0; d < 3; ++d) {
-    xl[d] = local_centre(p.x[3 * ip + d], p.origin[d], p.dx);
-    int a = (int)(xl[d] - r) - 2;
-    int b = (int)(xl[d] + r) + 2;
+    b.xl[d] = local_centre(p.x[3 * ip + d], p.origin[d], p.dx);
+    int a = (int)(b.xl[d] - r) - 2;
+    int c = (int)(b.xl[d] + r) + 2;
     if (d < 2 || g.dim == 3) {
       a = clampi(a, 1, g.L[d] - 1);
-      b = clampi(b, 1, g.L[d] - 1);
+      c = clampi(c, 1, g.L[d] - 1);
       if (d == 2) {
         if (a < 0) a = 0;
-        if (b < 1) b = 1;
+        if (c < 1) c = 1;
       }
     } else {
       // fmax(fmin(fmax(z, 1), nz - 1), slot) with nz = 1 in 2-D
       a = a < 1 ? 1 : a;
       a = a > g.L[2] - 1 ? g.L[2] - 1 : a;
       a = a < 0 ? 0 : a;
-      b = b < 1 ? 1 : b;
-      b = b > g.L[2] - 1 ? g.L[2] - 1 : b;
-      b = b < 1 ? 1 : b;
+      c = c < 1 ? 1 : c;
+      c = c > g.L[2] - 1 ? g.L[2] - 1 : c;
+      c = c < 1 ? 1 : c;
     }
-    lo[d] = a;
-    hi[d] = b;
+    b.lo[d] = a;
+    b.hi[d] = c;
   }
-  const int wx = hi[0] - lo[0], wy = hi[1] - lo[1], wz = hi[2] - lo[2];
-  double acc[12];
-#pragma unroll
-  for (int k = 0; k < 12; ++k) acc[k] = 0.0;
-  if (wx > 0 && wy > 0 && wz > 0) {
-    const long long total = (long long)wx * wy * wz;
-    const double ff = p.forceFactor, tf = p.torqueFactor;
-    for (long long t = threadIdx.x; t < total; t += RED_THREADS) {
-      const int k = lo[2] + (int)(t % wz);
-      const int j = lo[1] + (int)((t / wz) % wy);
-      const int i = lo[0] + (int)(t / ((long long)wz * wy));
-      const int sx = i - g.off[0], sy = j - g.off[1], sz = k - g.off[2];
-      const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
-      const int2 id = p.tab.ids[n];
-      int slot;
-      if (tag == id.x)
-        slot = 0;
-      else if (tag == id.y)
-        slot = 1;
-      else
-        continue;
-      double F0, F1, F2;
-      if (p.nodeF_is_double) {
-        const double* nf = static_cast<const double*>(p.tab.nodeF) + 6 * n + 3 * slot;
-        F0 = nf[0];
-        F1 = nf[1];
-        F2 = nf[2];
-      } else {
-        const float* nf = static_cast<const float*>(p.tab.nodeF) + 6 * n + 3 * slot;
-        F0 = nf[0];
-        F1 = nf[1];
-        F2 = nf[2];
-      }
-      acc[0] += F0 * ff;
-      acc[1] += F1 * ff;
-      acc[2] += F2 * ff;
-      const double dx = (double)i - xl[0];
-      const double dy = (double)j - xl[1];
-      const double dz = (double)k - xl[2];
-      acc[3] += (dy * F2 - dz * F1) * tf;
-      acc[4] += (dz * F0 - dx * F2) * tf;
-      acc[5] += (dx * F1 - dy * F0) * tf;
-      acc[6] += 0.5 * (dx * F0 + dx * F0) * tf;
-      acc[7] += 0.5 * (dy * F1 + dy * F1) * tf;
-      acc[8] += 0.5 * (dz * F2 + dz * F2) * tf;
-      acc[9] += 0.5 * (dy * F0 + dx * F1) * tf;
-      acc[10] += 0.5 * (dz * F0 + dx * F2) * tf;
-      acc[11] += 0.5 * (dz * F1 + dy * F2) * tf;
-    }
-  }
+  return b;
+}
+
+static __device__ __forceinline__ void block_reduce_store(double (&acc)[12], const ReduceParams& p,
+                                                          int ip) {
   // fixed-order reduction: butterfly within warps, then warps in index order
 #pragma unroll
   for (int k = 0; k < 12; ++k)
@@ -446,20 +610,133 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_kernel(ReduceParams p) {
   __syncthreads();
   if (threadIdx.x < 12) {
     const int k = threadIdx.x;
-    double s = 0.0;
-    for (int w = 0; w < RED_THREADS / 32; ++w) s += part[w][k];
+    double sum = 0.0;
+    for (int w = 0; w < RED_THREADS / 32; ++w) sum += part[w][k];
     if (k < 3)
-      p.fh[3 * ip + k] = s;
+      p.fh[3 * ip + k] = sum;
     else if (k < 6)
-      p.th[3 * ip + (k - 3)] = s;
+      p.th[3 * ip + (k - 3)] = sum;
     else
-      p.S[6 * ip + (k - 6)] = -s;
+      p.S[6 * ip + (k - 6)] = -sum;
   }
+}
+
+// FP64 node forces (FP64 storage): the reference's per-node terms in FP64.
+__global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p) {
+  const int ip = blockIdx.x;
+  const Geom& g = p.g;
+  const int tag = p.tag[ip];
+  const RedBox bx = reduce_box(p, ip);
+  const int wx = bx.hi[0] - bx.lo[0], wy = bx.hi[1] - bx.lo[1], wz = bx.hi[2] - bx.lo[2];
+  double acc[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) acc[k] = 0.0;
+  if (wx > 0 && wy > 0 && wz > 0) {
+    const long long total = (long long)wx * wy * wz;
+    const double ff = p.forceFactor, tf = p.torqueFactor;
+    const double* nodeF = static_cast<const double*>(p.tab.nodeF);
+    for (long long t = threadIdx.x; t < total; t += RED_THREADS) {
+      const int k = bx.lo[2] + (int)(t % wz);
+      const int j = bx.lo[1] + (int)((t / wz) % wy);
+      const int i = bx.lo[0] + (int)(t / ((long long)wz * wy));
+      const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
+      const int2 id = p.tab.ids[n];
+      int slot;
+      if (tag == id.x)
+        slot = 0;
+      else if (tag == id.y)
+        slot = 1;
+      else
+        continue;
+      const double* nf = nodeF + 6 * n + 3 * slot;
+      const double F0 = nf[0], F1 = nf[1], F2 = nf[2];
+      acc[0] += F0 * ff;
+      acc[1] += F1 * ff;
+      acc[2] += F2 * ff;
+      const double dx = (double)i - bx.xl[0];
+      const double dy = (double)j - bx.xl[1];
+      const double dz = (double)k - bx.xl[2];
+      acc[3] += (dy * F2 - dz * F1) * tf;
+      acc[4] += (dz * F0 - dx * F2) * tf;
+      acc[5] += (dx * F1 - dy * F0) * tf;
+      // 0.5*(a*b + a*b) is exactly a*b: doubling and halving are exact
+      acc[6] += (dx * F0) * tf;
+      acc[7] += (dy * F1) * tf;
+      acc[8] += (dz * F2) * tf;
+      acc[9] += 0.5 * (dy * F0 + dx * F1) * tf;
+      acc[10] += 0.5 * (dz * F0 + dx * F2) * tf;
+      acc[11] += 0.5 * (dz * F1 + dy * F2) * tf;
+    }
+  }
+  block_reduce_store(acc, p, ip);
+}
+
+// FP32 node forces (FP32 / FP16 storage): per-node terms and per-thread partial
+// sums in FP32 (the node forces carry FP32 precision), the per-particle sum
+// over threads in FP64.
+__global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p) {
+  const int ip = blockIdx.x;
+  const Geom& g = p.g;
+  const int tag = p.tag[ip];
+  const RedBox bx = reduce_box(p, ip);
+  const int wx = bx.hi[0] - bx.lo[0], wy = bx.hi[1] - bx.lo[1], wz = bx.hi[2] - bx.lo[2];
+  float a32[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) a32[k] = 0.0f;
+  if (wx > 0 && wy > 0 && wz > 0) {
+    int xi[3];
+    float xf[3];
+    for (int d = 0; d < 3; ++d) {
+      const double fl = fabs(bx.xl[d]) < 1.0e9 ? floor(bx.xl[d]) : 0.0;
+      xi[d] = (int)fl;
+      xf[d] = (float)(bx.xl[d] - fl);
+    }
+    const long long total = (long long)wx * wy * wz;
+    const float* nodeF = static_cast<const float*>(p.tab.nodeF);
+    for (long long t = threadIdx.x; t < total; t += RED_THREADS) {
+      const int k = bx.lo[2] + (int)(t % wz);
+      const int j = bx.lo[1] + (int)((t / wz) % wy);
+      const int i = bx.lo[0] + (int)(t / ((long long)wz * wy));
+      const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
+      const int2 id = p.tab.ids[n];
+      int slot;
+      if (tag == id.x)
+        slot = 0;
+      else if (tag == id.y)
+        slot = 1;
+      else
+        continue;
+      const float* nf = nodeF + 6 * n + 3 * slot;
+      const float F0 = nf[0], F1 = nf[1], F2 = nf[2];
+      const float dx = (float)(i - xi[0]) - xf[0];
+      const float dy = (float)(j - xi[1]) - xf[1];
+      const float dz = (float)(k - xi[2]) - xf[2];
+      a32[0] += F0;
+      a32[1] += F1;
+      a32[2] += F2;
+      a32[3] += dy * F2 - dz * F1;
+      a32[4] += dz * F0 - dx * F2;
+      a32[5] += dx * F1 - dy * F0;
+      a32[6] += dx * F0;
+      a32[7] += dy * F1;
+      a32[8] += dz * F2;
+      a32[9] += 0.5f * (dy * F0 + dx * F1);
+      a32[10] += 0.5f * (dz * F0 + dx * F2);
+      a32[11] += 0.5f * (dz * F1 + dy * F2);
+    }
+  }
+  double acc[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) acc[k] = (double)a32[k] * (k < 3 ? p.forceFactor : p.torqueFactor);
+  block_reduce_store(acc, p, ip);
 }
 
 cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st) {
   if (p.n <= 0) return cudaSuccess;
-  reduce_kernel<<<p.n, RED_THREADS, 0, st>>>(p);
+  if (p.nodeF_is_double)
+    reduce_f64_kernel<<<p.n, RED_THREADS, 0, st>>>(p);
+  else
+    reduce_f32_kernel<<<p.n, RED_THREADS, 0, st>>>(p);
   return cudaGetLastError();
 }
 
@@ -478,7 +755,7 @@ __global__ void table_export_kernel(Geom g, Table t, int* ids, double* eps, doub
   double2 e = make_double2(0.0, 0.0);
   double u[6] = {0, 0, 0, 0, 0, 0};
   if (ok) {
-    const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
+    const long long n = node_index(g, sx, sy, sz);
     id = t.ids[n];
     e = t.eps[n];
     for (int c = 0; c < 6; ++c) u[c] = t.us[6 * n + c];
@@ -514,7 +791,7 @@ __global__ void export_fields_kernel(Geom g, Table t, const double* rho, const d
   const int j = 1 + (int)((id / nxi) % nyi);
   const int k = (g.dim == 3 ? 1 : 0) + (int)(id / ((long long)nxi * nyi));
   const int sx = i - g.off[0], sy = j - g.off[1], sz = k - g.off[2];
-  const long long n = ((long long)sz * g.S[1] + sy) * g.S[0] + sx;
+  const long long n = node_index(g, sx, sy, sz);
   const double2 e = t.eps[n];
   const double Bv = (e.x + e.y);
   const double sv = (Bv > 1.0 ? 1.0 : Bv) * B0;
