@@ -58,6 +58,7 @@ struct lbmpsm_handle {
   unsigned long long* d_pair_total = nullptr;  // [0] list pairs, [1] codes
   int* d_status = nullptr;
   double* d_check = nullptr;
+  double* d_sf_value = nullptr;  // n/10^d for n = 0..1000
   void* h_stage = nullptr;  // pinned: inputs then outputs
   size_t h_stage_bytes = 0;
   int last_n = 0;
@@ -313,6 +314,11 @@ int collide(lbmpsm_handle* h) {
   p.invCs4 = h->invCs4;
   p.scale16 = h->scale16;
   p.status = h->d_status;
+  p.omega_f = (float)p.omega;
+  p.omo_f = (float)p.one_minus_omega;
+  p.gpref_f = (float)p.guo_pref;
+  p.tm_f = (float)(p.tau - 0.5);
+  for (int d = 0; d < 3; ++d) p.F_f[d] = (float)p.F[d];
   const int odd = (int)(h->t & 1);
   cudaError_t e;
   switch (h->opt.storage) {
@@ -370,6 +376,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     m.pair_total = h->d_pair_total;
     m.sfcode = h->d_sfcode;
     m.sf_cap = h->sf_cap;
+    m.sf_value = h->d_sf_value;
     m.status = h->d_status;
     m.write32 = h->opt.storage != LBMPSM_STORAGE_FP64 ? 1 : 0;
     CUDA_TRY(h, launch_map(m, h->stream));
@@ -570,8 +577,19 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
   if (dmalloc(h, &h->d_cells, sizeof(int) * 3 * (size_t)ncells) != cudaSuccess ||
       dmalloc(h, &h->d_pair_total, 2 * sizeof(unsigned long long)) != cudaSuccess ||
       dmalloc(h, &h->d_status, sizeof(int)) != cudaSuccess ||
-      dmalloc(h, &h->d_check, sizeof(double) * (4 + 4 * 1024)) != cudaSuccess)
+      dmalloc(h, &h->d_check, sizeof(double) * (4 + 4 * 1024)) != cudaSuccess ||
+      dmalloc(h, &h->d_sf_value, sizeof(double) * 1001) != cudaSuccess)
     return bail(LBMPSM_ERR_NOMEM);
+  {
+    // calcSolidFraction's return value fraction*n (src/LBM_PSM_exchangeParticleData.cpp:165,213)
+    double tbl[1001];
+    const int slices = 10;
+    double fraction = 1.0 / ((double)(slices * slices));
+    if (g.dim == 3) fraction = 1.0 / ((double)(slices * slices * slices));
+    for (int k = 0; k <= 1000; ++k) tbl[k] = fraction * ((double)k);
+    if (cudaMemcpy(h->d_sf_value, tbl, sizeof(tbl), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(LBMPSM_ERR_CUDA);
+  }
   cudaMemsetAsync(h->tab.flag, 0, N, h->stream);
   cudaMemsetAsync(h->tab.ids, 0, sizeof(int2) * N, h->stream);
   cudaMemsetAsync(h->tab.eps, 0, sizeof(double2) * N, h->stream);
@@ -611,6 +629,7 @@ void lbmpsm_destroy(lbmpsm_handle* h) {
   dfree(h->d_pair_total);
   dfree(h->d_status);
   dfree(h->d_check);
+  dfree(h->d_sf_value);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }

@@ -50,27 +50,29 @@ struct PsmNodeF {
   float F1[3], F2[3];
 };
 
+// Guo forcing term (src/LBM_PSM_dynamics.h:102-116) in deviation form
 template <class L, int q>
-__device__ __forceinline__ void collide_q_f32(float& gq, float drho, float rho, float ux,
-                                              float uy, float uz, float usq15, float omega,
-                                              float omo, float gpref, float Fx, float Fy,
-                                              float Fz, bool has_force, bool psm,
+__device__ __forceinline__ float guo_f32(float ux, float uy, float uz, float eu, float gpref,
+                                         float Fx, float Fy, float Fz) {
+  constexpr int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
+  const float w = (float)L::w(q);
+  const float a = ((float)cx - ux) * Fx + ((float)cy - uy) * Fy + ((float)cz - uz) * Fz;
+  const float eF = edotf<cx, cy, cz>(Fx, Fy, Fz);
+  return gpref * w * (3.0f * a + 9.0f * eu * eF);
+}
+
+// PSM collision of direction q (src/LBM_PSM_BGK_dynamics.h:70-113)
+template <class L, int q, bool FORCE>
+__device__ __forceinline__ void collide_q_psm(float& gq, float drho, float rho, float ux,
+                                              float uy, float uz, float usq15, float omo,
+                                              float gpref, float Fx, float Fy, float Fz,
                                               PsmNodeF& sn) {
   constexpr int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
   const float w = (float)L::w(q);
   const float g = gq;
   const float eu = edotf<cx, cy, cz>(ux, uy, uz);
   const float geq = w * (drho + rho * (3.0f * eu + 4.5f * eu * eu - usq15));
-  float Fq = 0.0f;
-  if (has_force) {
-    const float a = ((float)cx - ux) * Fx + ((float)cy - uy) * Fy + ((float)cz - uz) * Fz;
-    const float eF = edotf<cx, cy, cz>(Fx, Fy, Fz);
-    Fq = gpref * w * (3.0f * a + 9.0f * eu * eF);
-  }
-  if (!psm) {
-    gq = g + omega * (geq - g) + Fq;
-    return;
-  }
+  const float Fq = FORCE ? guo_f32<L, q>(ux, uy, uz, eu, gpref, Fx, Fy, Fz) : 0.0f;
   float sc1 = 0.0f, sc2 = 0.0f;
   if (sn.has1) {
     const float e1 = edotf<cx, cy, cz>(sn.us1[0], sn.us1[1], sn.us1[2]);
@@ -97,30 +99,50 @@ __device__ __forceinline__ void collide_q_f32(float& gq, float drho, float rho, 
   }
 }
 
-template <class L, int q>
-struct UnrollF {
-  __device__ __forceinline__ static void run(float* g, float drho, float rho, float ux,
-                                             float uy, float uz, float usq15, float omega,
-                                             float omo, float gpref, float Fx, float Fy,
-                                             float Fz, bool hf, bool psm, PsmNodeF& sn) {
-    collide_q_f32<L, q>(g[q], drho, rho, ux, uy, uz, usq15, omega, omo, gpref, Fx, Fy, Fz, hf,
-                        psm, sn);
-    UnrollF<L, q + 1>::run(g, drho, rho, ux, uy, uz, usq15, omega, omo, gpref, Fx, Fy, Fz, hf,
-                           psm, sn);
+template <class L, int q, bool FORCE>
+struct UnrollPsm {
+  __device__ __forceinline__ static void run(float* g, float drho, float rho, float ux, float uy,
+                                             float uz, float usq15, float omo, float gpref,
+                                             float Fx, float Fy, float Fz, PsmNodeF& sn) {
+    collide_q_psm<L, q, FORCE>(g[q], drho, rho, ux, uy, uz, usq15, omo, gpref, Fx, Fy, Fz, sn);
+    UnrollPsm<L, q + 1, FORCE>::run(g, drho, rho, ux, uy, uz, usq15, omo, gpref, Fx, Fy, Fz, sn);
   }
 };
-template <class L>
-struct UnrollF<L, L::Q> {
+template <class L, bool FORCE>
+struct UnrollPsm<L, L::Q, FORCE> {
   __device__ __forceinline__ static void run(float*, float, float, float, float, float, float,
-                                             float, float, float, float, float, float, bool,
-                                             bool, PsmNodeF&) {}
+                                             float, float, float, float, float, PsmNodeF&) {}
 };
 
-// Collision of one node on its 19 (or 9) deviations f[], in place: macro
-// values, optional macro store, PSM solid operator with node forces, Guo term.
-template <class L>
+// plain BGK collision of every direction with the Guo term
+template <class L, int q, bool FORCE>
+struct UnrollFluid {
+  __device__ __forceinline__ static void run(float* g, float drho, float rho, float ux, float uy,
+                                             float uz, float usq15, float omega, float gpref,
+                                             float Fx, float Fy, float Fz) {
+    constexpr int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
+    const float w = (float)L::w(q);
+    const float eu = edotf<cx, cy, cz>(ux, uy, uz);
+    const float geq = w * (drho + rho * (3.0f * eu + 4.5f * eu * eu - usq15));
+    const float Fq = FORCE ? guo_f32<L, q>(ux, uy, uz, eu, gpref, Fx, Fy, Fz) : 0.0f;
+    g[q] = g[q] + omega * (geq - g[q]) + Fq;
+    UnrollFluid<L, q + 1, FORCE>::run(g, drho, rho, ux, uy, uz, usq15, omega, gpref, Fx, Fy, Fz);
+  }
+};
+template <class L, bool FORCE>
+struct UnrollFluid<L, L::Q, FORCE> {
+  __device__ __forceinline__ static void run(float*, float, float, float, float, float, float,
+                                             float, float, float, float, float) {}
+};
+
+// Collision of one node on its Q deviations f[], in place: macro values,
+// optional macro store, then either the plain BGK update (fluid node) or the
+// PSM solid operator with node forces.  flag / r1 / r2 are the node's table
+// entries, loaded by the caller.
+template <class L, bool FORCE>
 __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const CollideParams& p,
-                                                  long long n) {
+                                                  long long n, uint8_t flag, float4 r1,
+                                                  float4 r2) {
   constexpr int Q = L::Q;
   float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
 #pragma unroll
@@ -131,12 +153,14 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
     if (cy) jy += cy > 0 ? f[q] : -f[q];
     if (cz) jz += cz > 0 ? f[q] : -f[q];
   }
-  const float Fx = (float)p.F[0], Fy = (float)p.F[1], Fz = (float)p.F[2];
-  jx += 0.5f * Fx;
-  jy += 0.5f * Fy;
-  jz += 0.5f * Fz;
+  const float Fx = p.F_f[0], Fy = p.F_f[1], Fz = p.F_f[2];
+  if (FORCE) {
+    jx += 0.5f * Fx;
+    jy += 0.5f * Fy;
+    jz += 0.5f * Fz;
+  }
   const float rho = 1.0f + drho;
-  const float inv = 1.0f / rho;
+  const float inv = __frcp_rn(rho);
   const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
   if (p.store_macro) {
     p.rho_out[n] = 1.0 + (double)drho;
@@ -145,65 +169,52 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
     p.u_out[3 * n + 2] = uz;
   }
   const float usq15 = 1.5f * (ux * ux + uy * uy + uz * uz);
-  const float omega = (float)p.omega;
-  const float omo = (float)p.one_minus_omega;
-
+  const float omega = p.omega_f;
+  if (flag == 0) {
+    UnrollFluid<L, 0, FORCE>::run(f, drho, rho, ux, uy, uz, usq15, omega, p.gpref_f, Fx, Fy, Fz);
+    return;
+  }
   PsmNodeF sn;
-  const uint8_t flag = p.tab.flag[n];
-  const bool psm = flag != 0;
   sn.has1 = (flag & 1) != 0;
   sn.has2 = (flag & 2) != 0;
 #pragma unroll
   for (int c = 0; c < 3; ++c) sn.F1[c] = sn.F2[c] = 0.0f;
-  if (psm) {
-    const float4 r1 = p.tab.rec32[2 * n];
-    const float4 r2 = p.tab.rec32[2 * n + 1];
-    float B1 = sn.has1 ? r1.x : 0.0f;
-    float B2 = sn.has2 ? r2.x : 0.0f;
-    if (p.weighting == 1) {
-      const float tm = (float)(p.tau - 0.5);
-      if (sn.has1) B1 = B1 * tm / ((1.0f - B1) + tm);
-      if (sn.has2) B2 = B2 * tm / ((1.0f - B2) + tm);
-    }
-    float Bt = B1 + B2;
-    if (Bt > 1.0f) {
-      B1 = B1 / Bt;
-      B2 = B2 / Bt;
-      Bt = 1.0f;
-    }
-    sn.B1 = B1;
-    sn.B2 = B2;
-    sn.omB = (1.0f - Bt) * omega;
-    sn.us1[0] = sn.has1 ? r1.y : 0.0f;
-    sn.us1[1] = sn.has1 ? r1.z : 0.0f;
-    sn.us1[2] = sn.has1 ? r1.w : 0.0f;
-    sn.us2[0] = sn.has2 ? r2.y : 0.0f;
-    sn.us2[1] = sn.has2 ? r2.z : 0.0f;
-    sn.us2[2] = sn.has2 ? r2.w : 0.0f;
-    sn.q1 = 1.5f * (sn.us1[0] * sn.us1[0] + sn.us1[1] * sn.us1[1] + sn.us1[2] * sn.us1[2]);
-    sn.q2 = 1.5f * (sn.us2[0] * sn.us2[0] + sn.us2[1] * sn.us2[1] + sn.us2[2] * sn.us2[2]);
-  } else {
-    sn.B1 = sn.B2 = 0.0f;
-    sn.omB = omega;
-    sn.q1 = sn.q2 = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) sn.us1[c] = sn.us2[c] = 0.0f;
+  float B1 = sn.has1 ? r1.x : 0.0f;
+  float B2 = sn.has2 ? r2.x : 0.0f;
+  if (p.weighting == 1) {  // Noble-Torczynski weighting (opt-in)
+    const float tm = p.tm_f;
+    if (sn.has1) B1 = B1 * tm / ((1.0f - B1) + tm);
+    if (sn.has2) B2 = B2 * tm / ((1.0f - B2) + tm);
   }
-  UnrollF<L, 0>::run(f, drho, rho, ux, uy, uz, usq15, omega, omo, (float)p.guo_pref, Fx, Fy, Fz,
-                     p.has_force != 0, psm, sn);
-  if (psm) {
-    float* nf = static_cast<float*>(p.tab.nodeF) + 6 * n;
+  float Bt = B1 + B2;
+  if (Bt > 1.0f) {
+    B1 = B1 / Bt;
+    B2 = B2 / Bt;
+    Bt = 1.0f;
+  }
+  sn.B1 = B1;
+  sn.B2 = B2;
+  sn.omB = (1.0f - Bt) * omega;
+  sn.us1[0] = sn.has1 ? r1.y : 0.0f;
+  sn.us1[1] = sn.has1 ? r1.z : 0.0f;
+  sn.us1[2] = sn.has1 ? r1.w : 0.0f;
+  sn.us2[0] = sn.has2 ? r2.y : 0.0f;
+  sn.us2[1] = sn.has2 ? r2.z : 0.0f;
+  sn.us2[2] = sn.has2 ? r2.w : 0.0f;
+  sn.q1 = 1.5f * (sn.us1[0] * sn.us1[0] + sn.us1[1] * sn.us1[1] + sn.us1[2] * sn.us1[2]);
+  sn.q2 = 1.5f * (sn.us2[0] * sn.us2[0] + sn.us2[1] * sn.us2[1] + sn.us2[2] * sn.us2[2]);
+  UnrollPsm<L, 0, FORCE>::run(f, drho, rho, ux, uy, uz, usq15, p.omo_f, p.gpref_f, Fx, Fy, Fz, sn);
+  float* nf = static_cast<float*>(p.tab.nodeF) + 6 * n;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      nf[c] = sn.F1[c];
-      nf[3 + c] = sn.F2[c];
-    }
+  for (int c = 0; c < 3; ++c) {
+    nf[c] = sn.F1[c];
+    nf[3 + c] = sn.F2[c];
   }
 }
 
 // Direct variant: each thread gathers its node's populations from global
 // memory (used when an x-row is longer than one staged block).
-template <class L, typename T, bool ODD>
+template <class L, typename T, bool ODD, bool FORCE>
 __global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
   constexpr int Q = L::Q;
   const Geom& g = p.g;
@@ -231,7 +242,13 @@ __global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
       f[q] = ok ? Store<T>::load(F + L::opp(q) * Np + n + o, sc) : 0.0f;
     }
   }
-  collide_node_lowp<L>(f, p, n);
+  const uint8_t flag = p.tab.flag[n];
+  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r1;
+  if (flag) {
+    r1 = p.tab.rec32[2 * n];
+    r2 = p.tab.rec32[2 * n + 1];
+  }
+  collide_node_lowp<L, FORCE>(f, p, n, flag, r1, r2);
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
@@ -343,10 +360,9 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW, 4) collide_staged_kernel(Colli
   T* buf = reinterpret_cast<T*>(smem_raw);
   const unsigned bar = smem_addr(smem_raw + (size_t)Q * P0 * sizeof(T));
   const unsigned row_bytes = (unsigned)(P0 * sizeof(T));
-  const int row = blockIdx.x;
-  const int sy = row % g.S[1];
-  const int sz = row / g.S[1];
-  const long long own = (long long)row * P0;
+  const int sy = blockIdx.x;
+  const int sz = blockIdx.y;
+  const long long own = ((long long)sz * g.S[1] + sy) * P0;
   T* __restrict__ F = static_cast<T*>(p.f);
   const long long Np = g.Np;
   const float sc = p.scale16;
@@ -382,35 +398,48 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW, 4) collide_staged_kernel(Colli
   const bool vxm = x > 0 || g.per[0];
   const bool vxp = x < S0 - 1 || g.per[0];
 
-  bool ready = false;
-  for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it)
-    if (mbar_try_wait(bar, 0)) {
-      ready = true;
-      break;
+  // the node's particle-table entries, fetched while the bulk copies fly
+  const long long n = own + x;
+  uint8_t flag = 0;
+  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r1;
+  if (active) {
+    flag = p.tab.flag[n];
+    if (flag) {
+      r1 = p.tab.rec32[2 * n];
+      r2 = p.tab.rec32[2 * n + 1];
     }
-  if (!ready) {
-    if (threadIdx.x == 0) atomicOr(p.status, STATUS_TIMEOUT);
-    // let the copies already issued land before the block gives up its shared memory
-    for (long long it = 0; it < MBAR_SPIN_LIMIT && !mbar_try_wait(bar, 0); ++it) {
-    }
-    return;
   }
+  // one thread polls the mbarrier (bounded), the others wait at the block barrier
+  __shared__ int ready;
+  if (threadIdx.x == 0) {
+    int ok = 0;
+    for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it)
+      if (mbar_try_wait(bar, 0)) {
+        ok = 1;
+        break;
+      }
+    if (!ok) {
+      atomicOr(p.status, STATUS_TIMEOUT);
+      // let the copies already issued land before the block gives up its shared memory
+      for (long long it = 0; it < MBAR_SPIN_LIMIT && !mbar_try_wait(bar, 0); ++it) {
+      }
+    }
+    ready = ok;
+  }
+  __syncthreads();
+  if (!ready) return;
 
   float f[Q];
   if (active) {
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      constexpr int dummy = 0;
-      (void)dummy;
       const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
       // the source node x - e_q exists: row and x neighbour
       const bool ok = ((rows >> row_bit(-cy, -cz)) & 1u) && (cx == 0 || (cx > 0 ? vxm : vxp));
       const int xs = ODD ? (cx == 0 ? x : (cx > 0 ? xm : xp)) : x;
       f[q] = ok ? Store<T>::load(buf + q * P0 + xs, sc) : 0.0f;
     }
-    CollideParams pp = p;
-    pp.has_force = FORCE ? 1 : 0;
-    collide_node_lowp<L>(f, pp, own + x);
+    collide_node_lowp<L, FORCE>(f, p, n, flag, r1, r2);
   }
   __syncthreads();  // every input read before any output overwrites the rows
   if (active) {
@@ -445,10 +474,10 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW, 4) collide_staged_kernel(Colli
 
 template <class L, typename T>
 static cudaError_t launch_lowp(const CollideParams& p, int odd, cudaStream_t st) {
-  if (p.g.S[0] <= STAGED_MAX_ROW) {
+  if (p.g.S[0] <= STAGED_MAX_ROW && p.g.S[2] <= 65535) {
     const unsigned threads = (unsigned)((p.g.S[0] + 31) / 32 * 32);
     const size_t smem = (size_t)L::Q * p.g.P0 * sizeof(T) + 16;
-    const unsigned rows = (unsigned)((long long)p.g.S[1] * p.g.S[2]);
+    const dim3 rows((unsigned)p.g.S[1], (unsigned)p.g.S[2]);
     if (odd) {
       if (p.has_force)
         collide_staged_kernel<L, T, true, true><<<rows, threads, smem, st>>>(p);
@@ -464,10 +493,17 @@ static cudaError_t launch_lowp(const CollideParams& p, int odd, cudaStream_t st)
   }
   dim3 block(128);
   dim3 grid((unsigned)(((p.g.S[0] + block.x - 1) / block.x) * (long long)p.g.S[1] * p.g.S[2]));
-  if (odd)
-    collide_lowp_kernel<L, T, true><<<grid, block, 0, st>>>(p);
-  else
-    collide_lowp_kernel<L, T, false><<<grid, block, 0, st>>>(p);
+  if (odd) {
+    if (p.has_force)
+      collide_lowp_kernel<L, T, true, true><<<grid, block, 0, st>>>(p);
+    else
+      collide_lowp_kernel<L, T, true, false><<<grid, block, 0, st>>>(p);
+  } else {
+    if (p.has_force)
+      collide_lowp_kernel<L, T, false, true><<<grid, block, 0, st>>>(p);
+    else
+      collide_lowp_kernel<L, T, false, false><<<grid, block, 0, st>>>(p);
+  }
   return cudaGetLastError();
 }
 

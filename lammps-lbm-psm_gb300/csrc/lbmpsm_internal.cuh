@@ -167,7 +167,33 @@ struct CollideParams {
   double invCs2, invCs4;
   float scale16;          // FP16 storage: stored value = deviation * scale16
   int* status;            // error word (STATUS_*)
+  // FP32 copies made on the host (double->float conversions are slow on the device)
+  float omega_f, omo_f, gpref_f, tm_f;
+  float F_f[3];
 };
+
+// Exact small-integer to float conversion without the conversion unit:
+// valid for |k| < 2^22.
+__device__ __forceinline__ float small_int_to_float(int k) {
+  return __int_as_float(0x4B400000 + k) - 12582912.0f;
+}
+
+// Division by a runtime divisor without the conversion unit (integer
+// division otherwise goes through int/float conversions, which share the slow
+// FP64 pipe on this GPU): q = umulhi(n, ceil(2^32/d)), exact for n*d < 2^32
+// (checked exhaustively for d <= 4096, n < 2^22).
+struct FastDiv {
+  unsigned d, m;
+};
+__host__ __device__ __forceinline__ FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  f.d = d;
+  f.m = d > 1 ? 0xFFFFFFFFu / d + 1u : 0u;
+  return f;
+}
+__device__ __forceinline__ unsigned fast_div(unsigned n, const FastDiv& f) {
+  return f.d > 1 ? __umulhi(n, f.m) : n;
+}
 
 // Zou-He face list of one `fix lbm-psm-bc` keyword.
 enum FaceKind {
@@ -239,6 +265,7 @@ struct MapParams {
   unsigned long long* pair_total;  // [0] cell-list pairs, [1] solid-fraction codes
   unsigned short* sfcode;          // codes of all (image, box node) pairs
   long long sf_cap;
+  const double* sf_value;          // sf_value[n] = n/10^d (n = 0..1000), FP64
   int* status;
   int write32;        // also write the FP32 mirror
 };

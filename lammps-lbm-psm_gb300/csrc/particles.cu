@@ -232,9 +232,9 @@ static __device__ int subcell_count_exact_group8(bool valid, int dim, double dx,
 static __device__ __forceinline__ int classify_node(int hi, int hj, int hk, const Img& im,
                                                     float& dxf, float& dyf, float& dzf) {
   const float u = 5.9604644775390625e-08f;  // 2^-24
-  dxf = (float)(hi - im.xi[0]) - im.xf[0];
-  dyf = (float)(hj - im.xi[1]) - im.xf[1];
-  dzf = (float)(hk - im.xi[2]) - im.xf[2];
+  dxf = small_int_to_float(hi - im.xi[0]) - im.xf[0];
+  dyf = small_int_to_float(hj - im.xi[1]) - im.xf[1];
+  dzf = small_int_to_float(hk - im.xi[2]) - im.xf[2];
   const float d32 = dxf * dxf + dyf * dyf + dzf * dzf;
   const float ad = fabsf(dxf) + fabsf(dyf) + fabsf(dzf);
   const float m = 16.0f * u * (5.0f * d32 + 2.0f * ad + 1.0f + im.rP2f);
@@ -254,99 +254,23 @@ static __device__ __forceinline__ int classify_node(int hi, int hj, int hk, cons
   return -1;
 }
 
-// Sub-cell count of a shell node by an 8-lane group, in FP32 with a proven
-// margin.  The sub-cell sums A+B+C are formed with the innermost loop along the
-// axis most nearly tangent to the surface (smallest |d|), so that most rows
-// of 10 are entirely inside or outside and decided by one comparison with the
-// row's extreme (FP32 addition is monotone).  Per-term error |fa - A| <= 5u Ex^2
-// with Ex = |dx| + 2 (the FP32 sub-cell offsets are within 1.7u of the
-// reference's); sum error <= 7.1u Emax; margin 16u(Emax + r^2).  amb != 0 when
-// a sub-cell sum falls inside the margin (exact FP64 count needed).  All 32
-// lanes call it; lanes of groups without work pass valid = false.
-static __device__ void subcell_count_fast_group8(bool valid, int dim, float dxf, float dyf,
-                                                 float dzf, const Img& im, int sub, int& n_out,
-                                                 int& amb_out) {
-  const float u = 5.9604644775390625e-08f;
-  int n = 0, amb = 0;
-  if (valid) {
-    float da = dxf, db = dyf, dc = dzf;
-    if (dim == 3) {
-      const float ax = fabsf(dxf), ay = fabsf(dyf), az = fabsf(dzf);
-      if (ax <= ay && ax <= az) {
-        da = dyf; db = dzf; dc = dxf;
-      } else if (ay <= ax && ay <= az) {
-        da = dxf; db = dzf; dc = dyf;
-      }
-    }
-    const float Ea = fabsf(da) + 2.0f, Eb = fabsf(db) + 2.0f, Ec = fabsf(dc) + 2.0f;
-    const float R = im.rSqf;
-    // rows r = sub + 8k: (a, b) = (r / 10, r % 10), advanced incrementally
-    int a = sub / 10, b = sub % 10;
-    if (dim == 2) {
-      const float M = 16.0f * u * (Ea * Ea + Eb * Eb + R);
-      const float lo = R - M, hi = R + M;
-      for (int r = sub; r < 100; r += 8) {
-        const float ta = da + (-0.45f + 0.1f * (float)a);
-        const float tb = db + (-0.45f + 0.1f * (float)b);
-        const float t = ta * ta + tb * tb;
-        n += (t < lo);
-        amb += (t >= lo) & (t <= hi);
-        b += 8;
-        if (b >= 10) {
-          b -= 10;
-          ++a;
-        }
-      }
-    } else {
-      const float M = 16.0f * u * (Ea * Ea + Eb * Eb + Ec * Ec + R);
-      const float lo = R - M, hi = R + M;
-      float fc[10];
-      float cmin = 3.4e38f, cmax = 0.0f;
-#pragma unroll
-      for (int c = 0; c < 10; ++c) {
-        const float tc = dc + (float)(-0.5 + ((double)c + 0.5) * 0.1);
-        fc[c] = tc * tc;
-        cmin = fminf(cmin, fc[c]);
-        cmax = fmaxf(cmax, fc[c]);
-      }
-      for (int r = sub; r < 100; r += 8) {
-        const float ta = da + (-0.45f + 0.1f * (float)a);
-        const float tb = db + (-0.45f + 0.1f * (float)b);
-        const float s = ta * ta + tb * tb;
-        if (s + cmax < lo) {
-          n += 10;
-        } else if (!(s + cmin > hi)) {
-#pragma unroll
-          for (int c = 0; c < 10; ++c) {
-            const float t = s + fc[c];
-            n += (t < lo);
-            amb += (t >= lo) & (t <= hi);
-          }
-        }
-        b += 8;
-        if (b >= 10) {
-          b -= 10;
-          ++a;
-        }
-      }
-    }
-  }
-#pragma unroll
-  for (int o = 4; o > 0; o >>= 1) {
-    n += __shfl_xor_sync(0xffffffffu, n, o);
-    amb += __shfl_xor_sync(0xffffffffu, amb, o);
-  }
-  n_out = n;
-  amb_out = amb;
+constexpr int SF_THREADS = 256;
+constexpr int SF_ROUND = 2048;  // box nodes classified per round (queue capacity)
+constexpr int SF_WBUF = 64;     // per-warp buffer of crossing rows
+
+static __device__ __forceinline__ float sub_offset(int k) {
+  return -0.45f + 0.1f * small_int_to_float(k);  // within 1.7u of the reference's delta_k
 }
 
-constexpr int SF_THREADS = 256;
-constexpr int SF_ROUND = 2048;
-
 // Phase 1 of the map: solid-fraction codes of every node of every image box
-// (independent of image order).  One block per image; nodes are classified
-// by their threads, shell nodes queued in shared memory and counted by whole
-// warps.
+// (independent of image order).  One block per image.  Box nodes are
+// classified per thread; shell nodes go to a shared-memory queue and are then
+// counted one per lane: every lane walks its node's 100 rows of 10 sub-cells
+// in a warp-uniform loop, counting rows wholly inside in registers, and pushes
+// rows that cross the surface into a per-warp buffer that is drained 32 rows
+// at a time, one row per lane (so no lane idles on another's crossing row).
+// Nodes where any sub-cell sum falls inside the FP32 margin are recounted
+// exactly in FP64.
 __global__ void __launch_bounds__(SF_THREADS) sf_kernel(MapParams p) {
   const Img& im = p.img[blockIdx.x];
   if (!im.valid) return;
@@ -357,17 +281,30 @@ __global__ void __launch_bounds__(SF_THREADS) sf_kernel(MapParams p) {
   const int wx = im.box[0], wy = im.box[1], wz = im.box[2];
   const int vol = wx * wy * wz;
   unsigned short* code = p.sfcode + im.sf_off;
+  constexpr int NW = SF_THREADS / 32;
   __shared__ int queue[SF_ROUND];
-  __shared__ int qn;
+  __shared__ int exact_list[SF_ROUND];
+  __shared__ float buf_s[NW][SF_WBUF];
+  __shared__ int buf_o[NW][SF_WBUF];
+  __shared__ float np_dc[NW][32], np_lo[NW][32], np_hi[NW][32];
+  __shared__ int wcnt[NW][32], wamb[NW][32];
+  __shared__ int qn, nex;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float u = 5.9604644775390625e-08f;  // 2^-24
+  const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
   for (int base = 0; base < vol; base += SF_ROUND) {
-    if (threadIdx.x == 0) qn = 0;
+    if (threadIdx.x == 0) {
+      qn = 0;
+      nex = 0;
+    }
     __syncthreads();
     const int end = min(vol, base + SF_ROUND);
     for (int li = base + threadIdx.x; li < end; li += SF_THREADS) {
-      const int sx = im.lo[0] + li % wx;
-      const int sy = im.lo[1] + (li / wx) % wy;
-      const int sz = im.lo[2] + li / (wx * wy);
+      const int q1 = (int)fast_div((unsigned)li, fx);
+      const int q2 = (int)fast_div((unsigned)q1, fy);
+      const int sx = im.lo[0] + li - q1 * wx;
+      const int sy = im.lo[1] + q1 - q2 * wy;
+      const int sz = im.lo[2] + q2;
       float dxf, dyf, dzf;
       const int c = classify_node(sx + g.off[0], sy + g.off[1], sz + g.off[2], im, dxf, dyf, dzf);
       if (c >= 0)
@@ -377,27 +314,138 @@ __global__ void __launch_bounds__(SF_THREADS) sf_kernel(MapParams p) {
     }
     __syncthreads();
     const int nq = qn;
-    // four shell nodes per warp, one 8-lane group each
-    const int grp = lane >> 3, sub = lane & 7;
-    for (int e0 = warp * 4; e0 < nq; e0 += (SF_THREADS / 32) * 4) {
-      const int e = e0 + grp;
+    for (int e0 = warp * 32; e0 < nq; e0 += SF_THREADS) {
+      const int e = e0 + lane;
       const bool valid = e < nq;
-      const int li = valid ? queue[e] : 0;
-      const int hi = im.lo[0] + li % wx + g.off[0];
-      const int hj = im.lo[1] + (li / wx) % wy + g.off[1];
-      const int hk = im.lo[2] + li / (wx * wy) + g.off[2];
-      const float dxf = (float)(hi - im.xi[0]) - im.xf[0];
-      const float dyf = (float)(hj - im.xi[1]) - im.xf[1];
-      const float dzf = (float)(hk - im.xi[2]) - im.xf[2];
-      int nc, amb;
-      subcell_count_fast_group8(valid, g.dim, dxf, dyf, dzf, im, sub, nc, amb);
-      const bool need_exact = valid && amb != 0;
-      if (__any_sync(0xffffffffu, need_exact)) {
-        const int ne = subcell_count_exact_group8(need_exact, g.dim, (double)hi - im.xl[0],
-                                                  (double)hj - im.xl[1], (double)hk - im.xl[2],
-                                                  im.r, sub);
-        if (need_exact) nc = ne;
+      const int li = valid ? queue[e] : queue[e0];
+      const int q1 = (int)fast_div((unsigned)li, fx);
+      const int q2 = (int)fast_div((unsigned)q1, fy);
+      const float dxf = small_int_to_float(im.lo[0] + li - q1 * wx + g.off[0] - im.xi[0]) - im.xf[0];
+      const float dyf = small_int_to_float(im.lo[1] + q1 - q2 * wy + g.off[1] - im.xi[1]) - im.xf[1];
+      const float dzf = small_int_to_float(im.lo[2] + q2 + g.off[2] - im.xi[2]) - im.xf[2];
+      // axis order: outer a, middle b, inner c along the smallest |d|
+      float da = dxf, db = dyf, dc = dzf;
+      if (g.dim == 3) {
+        const float ax = fabsf(dxf), ay = fabsf(dyf), az = fabsf(dzf);
+        if (ax <= ay && ax <= az) {
+          da = dyf; db = dzf; dc = dxf;
+        } else if (ay <= ax && ay <= az) {
+          da = dxf; db = dzf; dc = dyf;
+        }
       }
+      const float Ea = fabsf(da) + 2.0f, Eb = fabsf(db) + 2.0f, Ec = fabsf(dc) + 2.0f;
+      const float Emax = g.dim == 3 ? Ea * Ea + Eb * Eb + Ec * Ec : Ea * Ea + Eb * Eb;
+      const float M = 16.0f * u * (Emax + im.rSqf);
+      const float lo = im.rSqf - M, hi = im.rSqf + M;
+      int n = 0, amb = 0;
+      if (g.dim == 2) {
+        for (int a = 0; a < 10; ++a) {
+          const float ta = da + sub_offset(a);
+          const float sa = ta * ta;
+#pragma unroll
+          for (int b = 0; b < 10; ++b) {
+            const float tb = db + (float)(-0.5 + ((double)b + 0.5) * 0.1);
+            const float t = sa + tb * tb;
+            n += (t < lo);
+            amb += (t >= lo) & (t <= hi);
+          }
+        }
+      } else {
+        float cmin = 3.4e38f, cmax = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) {
+          const float t = dc + (float)(-0.5 + ((double)k + 0.5) * 0.1);
+          cmin = fminf(cmin, t * t);
+          cmax = fmaxf(cmax, t * t);
+        }
+        np_dc[warp][lane] = dc;
+        np_lo[warp][lane] = lo;
+        np_hi[warp][lane] = hi;
+        wcnt[warp][lane] = 0;
+        wamb[warp][lane] = 0;
+        __syncwarp();
+        int wcount = 0;
+        for (int a = 0; a < 10; ++a) {
+          const float ta = da + sub_offset(a);
+          const float sa = ta * ta;
+          for (int b = 0; b < 10; ++b) {
+            const float tb = db + sub_offset(b);
+            const float sv = sa + tb * tb;
+            const bool inside = sv + cmax < lo;
+            const bool cross = valid && !inside && !(sv + cmin > hi);
+            n += inside ? 10 : 0;
+            const unsigned m = __ballot_sync(0xffffffffu, cross);
+            if (cross) {
+              const int pos = wcount + __popc(m & ((1u << lane) - 1u));
+              buf_s[warp][pos] = sv;
+              buf_o[warp][pos] = lane;
+            }
+            wcount += __popc(m);
+            if (wcount >= 32) {
+              __syncwarp();
+              const int k = wcount - 32 + lane;
+              const float sk = buf_s[warp][k];
+              const int ow = buf_o[warp][k];
+              const float dco = np_dc[warp][ow], loo = np_lo[warp][ow], hio = np_hi[warp][ow];
+              int nn = 0, na = 0;
+#pragma unroll
+              for (int cc = 0; cc < 10; ++cc) {
+                const float tc = dco + (float)(-0.5 + ((double)cc + 0.5) * 0.1);
+                const float t = sk + tc * tc;
+                nn += (t < loo);
+                na += (t >= loo) & (t <= hio);
+              }
+              if (nn) atomicAdd(&wcnt[warp][ow], nn);
+              if (na) atomicAdd(&wamb[warp][ow], na);
+              wcount -= 32;
+              __syncwarp();
+            }
+          }
+        }
+        __syncwarp();
+        if (lane < wcount) {
+          const float sk = buf_s[warp][lane];
+          const int ow = buf_o[warp][lane];
+          const float dco = np_dc[warp][ow], loo = np_lo[warp][ow], hio = np_hi[warp][ow];
+          int nn = 0, na = 0;
+#pragma unroll
+          for (int cc = 0; cc < 10; ++cc) {
+            const float tc = dco + (float)(-0.5 + ((double)cc + 0.5) * 0.1);
+            const float t = sk + tc * tc;
+            nn += (t < loo);
+            na += (t >= loo) & (t <= hio);
+          }
+          if (nn) atomicAdd(&wcnt[warp][ow], nn);
+          if (na) atomicAdd(&wamb[warp][ow], na);
+        }
+        __syncwarp();
+        n += wcnt[warp][lane];
+        amb += wamb[warp][lane];
+        __syncwarp();
+      }
+      if (valid) {
+        if (amb == 0)
+          code[li] = (unsigned short)n;
+        else
+          exact_list[atomicAdd(&nex, 1)] = li;
+      }
+    }
+    __syncthreads();
+    // exact FP64 recount of the ambiguous nodes, four per warp
+    const int ne = nex;
+    const int grp = lane >> 3, sub = lane & 7;
+    for (int e0 = warp * 4; e0 < ne; e0 += NW * 4) {
+      const int e = e0 + grp;
+      const bool valid = e < ne;
+      const int li = valid ? exact_list[e] : 0;
+      const int q1 = (int)fast_div((unsigned)li, fx);
+      const int q2 = (int)fast_div((unsigned)q1, fy);
+      const int hi = im.lo[0] + li - q1 * wx + g.off[0];
+      const int hj = im.lo[1] + q1 - q2 * wy + g.off[1];
+      const int hk = im.lo[2] + q2 + g.off[2];
+      const int nc = subcell_count_exact_group8(valid, g.dim, (double)hi - im.xl[0],
+                                                (double)hj - im.xl[1], (double)hk - im.xl[2],
+                                                im.r, sub);
       if (valid && sub == 0) code[li] = (unsigned short)nc;
     }
     __syncthreads();
@@ -409,24 +457,30 @@ __global__ void __launch_bounds__(SF_THREADS) sf_kernel(MapParams p) {
 // (src/LBM_PSM_exchangeParticleData.cpp:69-106) on the two-slot table
 // (setParticleOnLattice / setToZero, src/LBM_PSM_lattice.cpp:257-324).
 // The table is written back only where it changed.
+// Phase 2 of the map, per node: the images whose boxes contain it, in image
+// order (the cell list is sorted), through the update of setParticlesOnLattice
+// (src/LBM_PSM_exchangeParticleData.cpp:69-106) on the two-slot table
+// (setParticleOnLattice / setToZero, src/LBM_PSM_lattice.cpp:257-324).
+// decFlag = (sf > 1e-5) + 2*(sf_old > 1e-5): cases 0 and 2 clear the tag's slot
+// (case 0 finds none unless the tag is the empty marker 0), cases 1 and 3 set
+// it (case 3's condition sf > sf_old || id_old == tag holds because
+// sf_old > 1e-5 means the tag matched), so only the sf bit decides.  sf > 1e-5
+// exactly when the code is non-zero.  The table is written back only where it
+// changed.
 __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
-  const int c = blockIdx.x;
+  const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
   const int cnt = p.cell_count[c];
   if (cnt == 0) return;
   if (p.pair_total[0] > (unsigned long long)p.list_cap ||
       p.pair_total[1] > (unsigned long long)p.sf_cap)
     return;
   const Geom& g = p.g;
-  const int cx = c % p.C[0];
-  const int cy = (c / p.C[0]) % p.C[1];
-  const int cz = c / (p.C[0] * p.C[1]);
-  const int sx = cx * p.cb[0] + threadIdx.x;
-  const int sy = cy * p.cb[1] + threadIdx.y;
-  const int sz = cz * p.cb[2] + threadIdx.z;
+  const int sx = blockIdx.x * p.cb[0] + threadIdx.x;
+  const int sy = blockIdx.y * p.cb[1] + threadIdx.y;
+  const int sz = blockIdx.z * p.cb[2] + threadIdx.z;
   if (sx >= g.S[0] || sy >= g.S[1] || sz >= g.S[2]) return;
   const long long n = node_index(g, sx, sy, sz);
   const int hi = sx + g.off[0], hj = sy + g.off[1], hk = sz + g.off[2];
-  const double fraction = g.dim == 3 ? 1.0 / ((double)(10 * 10 * 10)) : 1.0 / ((double)(10 * 10));
   const int* lst = p.list + p.cell_off[c];
   int id[2] = {0, 0};
   double eps[2] = {0.0, 0.0};
@@ -438,96 +492,83 @@ __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
     if (sx < im.lo[0] || sx >= im.hi[0] || sy < im.lo[1] || sy >= im.hi[1] || sz < im.lo[2] ||
         sz >= im.hi[2])
       continue;
+    const int li = ((sz - im.lo[2]) * im.box[1] + (sy - im.lo[1])) * im.box[0] + (sx - im.lo[0]);
+    const unsigned short cd = p.sfcode[im.sf_off + li];
+    const int tag = im.tag;
     if (!have_ids) {
       const int2 v = p.tab.ids[n];
       id[0] = v.x;
       id[1] = v.y;
       have_ids = true;
     }
-    const int tag = im.tag;
-    const int li = ((sz - im.lo[2]) * im.box[1] + (sy - im.lo[1])) * im.box[0] + (sx - im.lo[0]);
-    const unsigned short cd = p.sfcode[im.sf_off + li];
-    // sf = n/10^d (or the early-out 1.0) exceeds 1e-5 exactly when n > 0
-    const bool sf_pos = cd != 0;
     const int match = tag == id[0] ? 0 : (tag == id[1] ? 1 : -1);
-    bool old_pos = false;
-    if (match >= 0) {
-      if (!have_eps) {
-        const double2 e = p.tab.eps[n];
-        eps[0] = e.x;
-        eps[1] = e.y;
-        have_eps = true;
-      }
-      old_pos = eps[match] > 0.00001;
-    }
-    // decFlag = (sf > 1e-5) + 2*(sf_old > 1e-5); sf_old > 1e-5 implies the tag
-    // holds a slot (id_old == tag), which makes case 3 always set and case 2
-    // always clear
-    const int decFlag = (sf_pos ? 1 : 0) + (old_pos ? 2 : 0);
-    int set = -2;  // -2: nothing, -1: clear the tag, 0: set
-    switch (decFlag) {
-      case 0:
-        set = -1;
-        break;
-      case 1:
-        set = 0;
-        break;
-      case 2:
-        set = -1;
-        break;
-      case 3:
-        set = 0;
-        break;
-    }
-    if (set == -1 && match >= 0) {  // setToZero
-      if (!have_eps) {
-        const double2 e = p.tab.eps[n];
-        eps[0] = e.x;
-        eps[1] = e.y;
-        have_eps = true;
-      }
-      id[match] = 0;
-      eps[match] = 0.0;
-      us[3 * match] = us[3 * match + 1] = us[3 * match + 2] = 0.0;
-      ids_dirty = true;
-      slot_dirty[match] = true;
-    } else if (set == 0) {  // setParticleOnLattice: matching slot, else first empty, else drop
-      int slot = -1;
-      if (id[0] == tag)
-        slot = 0;
-      else if (id[1] == tag)
-        slot = 1;
-      else if (id[0] == 0)
-        slot = 0;
-      else if (id[1] == 0)
-        slot = 1;
-      if (slot >= 0) {
+    if (cd == 0) {  // setToZero (src/LBM_PSM_lattice.cpp:302-324)
+      if (match >= 0) {
         if (!have_eps) {
           const double2 e = p.tab.eps[n];
           eps[0] = e.x;
           eps[1] = e.y;
           have_eps = true;
         }
-        if (id[slot] != tag) ids_dirty = true;
-        id[slot] = tag;
-        eps[slot] = cd == SF_ONE ? 1.0 : fraction * ((double)cd);
-        // rigid-body velocity of the node (src/LBM_PSM_exchangeParticleData.cpp:83-89)
-        if (im.has_spin) {
-          const double dx = (double)hi - im.xl[0];
-          const double dy = (double)hj - im.xl[1];
-          const double dz = (double)hk - im.xl[2];
-          us[3 * slot + 0] = im.uT[0] + im.om[1] * dz - im.om[2] * dy;
-          us[3 * slot + 1] = im.uT[1] + im.om[2] * dx - im.om[0] * dz;
-          us[3 * slot + 2] = im.uT[2] + im.om[0] * dy - im.om[1] * dx;
-        } else {
-          // with omega == 0 the cross-product terms are signed zeros: the
-          // reference's (uT + 0*dz) - 0*dy equals uT + 0.0 bit for bit
-          us[3 * slot + 0] = im.uT[0] + 0.0;
-          us[3 * slot + 1] = im.uT[1] + 0.0;
-          us[3 * slot + 2] = im.uT[2] + 0.0;
-        }
-        slot_dirty[slot] = true;
+        id[match] = 0;
+        eps[match] = 0.0;
+        us[3 * match] = us[3 * match + 1] = us[3 * match + 2] = 0.0;
+        ids_dirty = true;
+        slot_dirty[match] = true;
       }
+      continue;
+    }
+    // setParticleOnLattice: matching slot, else the first empty one, else drop
+    int slot = -1;
+    if (id[0] == tag)
+      slot = 0;
+    else if (id[1] == tag)
+      slot = 1;
+    else if (id[0] == 0)
+      slot = 0;
+    else if (id[1] == 0)
+      slot = 1;
+    if (slot < 0) continue;
+    if (!have_eps) {
+      const double2 e = p.tab.eps[n];
+      eps[0] = e.x;
+      eps[1] = e.y;
+      have_eps = true;
+    }
+    const double sf = cd == SF_ONE ? 1.0 : p.sf_value[cd];
+    // rigid-body velocity of the node (src/LBM_PSM_exchangeParticleData.cpp:83-89)
+    double u0, u1, u2;
+    if (im.has_spin) {
+      const double dx = (double)hi - im.xl[0];
+      const double dy = (double)hj - im.xl[1];
+      const double dz = (double)hk - im.xl[2];
+      u0 = im.uT[0] + im.om[1] * dz - im.om[2] * dy;
+      u1 = im.uT[1] + im.om[2] * dx - im.om[0] * dz;
+      u2 = im.uT[2] + im.om[0] * dy - im.om[1] * dx;
+    } else {
+      // every omega component +0.0 and no uT component -0.0: the reference's
+      // (uT + 0*dz) - 0*dy is uT bit for bit
+      u0 = im.uT[0];
+      u1 = im.uT[1];
+      u2 = im.uT[2];
+    }
+    // re-setting a slot to the values it already holds changes nothing
+    bool same = !slot_dirty[slot] && id[slot] == tag &&
+                __double_as_longlong(eps[slot]) == __double_as_longlong(sf);
+    if (same) {
+      const double* cur = p.tab.us + 6 * n + 3 * slot;
+      same = __double_as_longlong(cur[0]) == __double_as_longlong(u0) &&
+             __double_as_longlong(cur[1]) == __double_as_longlong(u1) &&
+             __double_as_longlong(cur[2]) == __double_as_longlong(u2);
+    }
+    if (!same) {
+      if (id[slot] != tag) ids_dirty = true;
+      id[slot] = tag;
+      eps[slot] = sf;
+      us[3 * slot + 0] = u0;
+      us[3 * slot + 1] = u1;
+      us[3 * slot + 2] = u2;
+      slot_dirty[slot] = true;
     }
   }
   if (ids_dirty) {
@@ -554,7 +595,8 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   cell_sort_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(p, ncells);
   sf_kernel<<<p.n, SF_THREADS, 0, st>>>(p);
   dim3 block(p.cb[0], p.cb[1], p.cb[2]);
-  node_apply_kernel<<<ncells, block, 0, st>>>(p);
+  dim3 cells((unsigned)p.C[0], (unsigned)p.C[1], (unsigned)p.C[2]);
+  node_apply_kernel<<<cells, block, 0, st>>>(p);
   return cudaGetLastError();
 }
 
@@ -635,10 +677,13 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
     const long long total = (long long)wx * wy * wz;
     const double ff = p.forceFactor, tf = p.torqueFactor;
     const double* nodeF = static_cast<const double*>(p.tab.nodeF);
+    const FastDiv fz = make_fastdiv((unsigned)wz), fy = make_fastdiv((unsigned)wy);
     for (long long t = threadIdx.x; t < total; t += RED_THREADS) {
-      const int k = bx.lo[2] + (int)(t % wz);
-      const int j = bx.lo[1] + (int)((t / wz) % wy);
-      const int i = bx.lo[0] + (int)(t / ((long long)wz * wy));
+      const int q1 = (int)fast_div((unsigned)t, fz);
+      const int q2 = (int)fast_div((unsigned)q1, fy);
+      const int k = bx.lo[2] + (int)t - q1 * wz;
+      const int j = bx.lo[1] + q1 - q2 * wy;
+      const int i = bx.lo[0] + q2;
       const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
       const int2 id = p.tab.ids[n];
       int slot;
@@ -671,18 +716,28 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
   block_reduce_store(acc, p, ip);
 }
 
-// FP32 node forces (FP32 / FP16 storage): per-node terms and per-thread partial
-// sums in FP32 (the node forces carry FP32 precision), the per-particle sum
-// over threads in FP64.
+// Error-free transformation: a + b = s + e exactly (Knuth's TwoSum; no
+// contraction or reassociation under -fmad=false).
+static __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// FP32 node forces (FP32 / FP16 storage): per-node terms in FP32 (the node
+// forces carry FP32 precision), accumulated per particle in double-float
+// (hi + lo pairs combined with TwoSum, ~48-bit significand) on the FP32 pipe,
+// then the per-warp results summed in FP64.  (FP64 arithmetic runs at 1/64 of
+// the FP32 rate on this GPU.)
 __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p) {
   const int ip = blockIdx.x;
   const Geom& g = p.g;
   const int tag = p.tag[ip];
   const RedBox bx = reduce_box(p, ip);
   const int wx = bx.hi[0] - bx.lo[0], wy = bx.hi[1] - bx.lo[1], wz = bx.hi[2] - bx.lo[2];
-  float a32[12];
+  float hi[12], lo[12];
 #pragma unroll
-  for (int k = 0; k < 12; ++k) a32[k] = 0.0f;
+  for (int k = 0; k < 12; ++k) hi[k] = lo[k] = 0.0f;
   if (wx > 0 && wy > 0 && wz > 0) {
     int xi[3];
     float xf[3];
@@ -691,12 +746,15 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
       xi[d] = (int)fl;
       xf[d] = (float)(bx.xl[d] - fl);
     }
-    const long long total = (long long)wx * wy * wz;
+    const int total = wx * wy * wz;
     const float* nodeF = static_cast<const float*>(p.tab.nodeF);
-    for (long long t = threadIdx.x; t < total; t += RED_THREADS) {
-      const int k = bx.lo[2] + (int)(t % wz);
-      const int j = bx.lo[1] + (int)((t / wz) % wy);
-      const int i = bx.lo[0] + (int)(t / ((long long)wz * wy));
+    const FastDiv fz = make_fastdiv((unsigned)wz), fy = make_fastdiv((unsigned)wy);
+    for (int t = threadIdx.x; t < total; t += RED_THREADS) {
+      const int q1 = (int)fast_div((unsigned)t, fz);
+      const int q2 = (int)fast_div((unsigned)q1, fy);
+      const int k = bx.lo[2] + t - q1 * wz;
+      const int j = bx.lo[1] + q1 - q2 * wy;
+      const int i = bx.lo[0] + q2;
       const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
       const int2 id = p.tab.ids[n];
       int slot;
@@ -708,27 +766,59 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
         continue;
       const float* nf = nodeF + 6 * n + 3 * slot;
       const float F0 = nf[0], F1 = nf[1], F2 = nf[2];
-      const float dx = (float)(i - xi[0]) - xf[0];
-      const float dy = (float)(j - xi[1]) - xf[1];
-      const float dz = (float)(k - xi[2]) - xf[2];
-      a32[0] += F0;
-      a32[1] += F1;
-      a32[2] += F2;
-      a32[3] += dy * F2 - dz * F1;
-      a32[4] += dz * F0 - dx * F2;
-      a32[5] += dx * F1 - dy * F0;
-      a32[6] += dx * F0;
-      a32[7] += dy * F1;
-      a32[8] += dz * F2;
-      a32[9] += 0.5f * (dy * F0 + dx * F1);
-      a32[10] += 0.5f * (dz * F0 + dx * F2);
-      a32[11] += 0.5f * (dz * F1 + dy * F2);
+      const float dx = small_int_to_float(i - xi[0]) - xf[0];
+      const float dy = small_int_to_float(j - xi[1]) - xf[1];
+      const float dz = small_int_to_float(k - xi[2]) - xf[2];
+      const float term[12] = {F0,
+                              F1,
+                              F2,
+                              dy * F2 - dz * F1,
+                              dz * F0 - dx * F2,
+                              dx * F1 - dy * F0,
+                              dx * F0,
+                              dy * F1,
+                              dz * F2,
+                              0.5f * (dy * F0 + dx * F1),
+                              0.5f * (dz * F0 + dx * F2),
+                              0.5f * (dz * F1 + dy * F2)};
+#pragma unroll
+      for (int q = 0; q < 12; ++q) {
+        float sv, e;
+        two_sum(hi[q], term[q], sv, e);
+        hi[q] = sv;
+        lo[q] += e;
+      }
     }
   }
-  double acc[12];
+  // fixed-order double-float butterfly within the warp
 #pragma unroll
-  for (int k = 0; k < 12; ++k) acc[k] = (double)a32[k] * (k < 3 ? p.forceFactor : p.torqueFactor);
-  block_reduce_store(acc, p, ip);
+  for (int q = 0; q < 12; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, hi[q], o);
+      const float l2 = __shfl_xor_sync(0xffffffffu, lo[q], o);
+      float sv, e;
+      two_sum(hi[q], h2, sv, e);
+      hi[q] = sv;
+      lo[q] = lo[q] + l2 + e;
+    }
+  }
+  __shared__ double part[RED_THREADS / 32][12];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int q = 0; q < 12; ++q) part[warp][q] = (double)hi[q] + (double)lo[q];
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    const int q = threadIdx.x;
+    double sum = 0.0;
+    for (int w = 0; w < RED_THREADS / 32; ++w) sum += part[w][q];
+    if (q < 3)
+      p.fh[3 * ip + q] = sum * p.forceFactor;
+    else if (q < 6)
+      p.th[3 * ip + (q - 3)] = sum * p.torqueFactor;
+    else
+      p.S[6 * ip + (q - 6)] = -(sum * p.torqueFactor);
+  }
 }
 
 cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st) {
