@@ -197,6 +197,24 @@ int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps);
 /* Copy the per-image outputs of the last step to host memory. */
 int lbmpsm_read_forces(lbmpsm_handle* h, int n, double* fh, double* th, double* stresslet);
 
+/* Allocation-free variant of lbmpsm_export_fields; no counterpart in the
+ * reference.  For callers that cannot allocate device memory while a run is
+ * under way: a host program whose pool allocator already holds nearly all of
+ * HBM, or one whose other streams on the GPU must not be stalled by the
+ * device-wide wait of cudaFree.  Same arguments and output as
+ * lbmpsm_export_fields, staged through one fixed device array of
+ * LBMPSM_EXPORT_STATIC_MAX_BYTES that every GPU loading the library holds
+ * until exit; the requested fields must fit in it (float output: 4 bytes per
+ * node per component, double 8; solid and rho one component, u three),
+ * otherwise the call returns LBMPSM_ERR_CAPACITY and allocates nothing.  The
+ * first call on each device looks up the array's device address; make it
+ * before any stream capture begins.  Calls share the array; the library
+ * serialises them with a process-wide lock held until each call's copies
+ * have finished.  Synchronous, like lbmpsm_export_fields. */
+#define LBMPSM_EXPORT_STATIC_MAX_BYTES (64u * 1024u * 1024u)
+int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, double B0, double rho0,
+                                double u0, void* solid, void* rho, void* u);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -915,3 +916,77 @@ int lbmpsm_read_forces(lbmpsm_handle* h, int n, double* fh, double* th, double* 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free field export (lbmpsm_export_fields_static).
+//
+// lbmpsm_export_fields stages the fields through a device buffer that it
+// cudaMalloc's and cudaFree's on every call.  Two kinds of caller cannot
+// allow that in the middle of a run: a host program whose own pool allocator
+// already holds nearly all of HBM, so that the cudaMalloc fails, and one that
+// runs other streams on the same GPU, which cudaFree would stall because it
+// waits for the whole device.  This variant stages through the fixed array
+// below: LBMPSM_EXPORT_STATIC_MAX_BYTES (64 MiB) that every GPU loading the
+// library holds until the process exits.  It launches the same export kernel
+// as lbmpsm_export_fields and allocates nothing.
+//
+// In host code g_export_scratch only stands for the device array; its device
+// address is looked up with cudaGetSymbolAddress once per device, with that
+// device current, on the first call made for a handle on that device.  Make
+// that first call before any stream capture begins.
+//
+// Every call on a device uses the same array and leaves its contents there.
+// Nothing in it has to start at zero: the kernel writes every element that
+// the copies then read back, so a previous call's data never reaches the
+// caller.  Exports whose GPU work overlapped would race on the array; this
+// function therefore holds a process-wide lock from its launch until its
+// copies have finished, so its own calls run one after another.
+static __device__ __align__(256) unsigned char g_export_scratch[LBMPSM_EXPORT_STATIC_MAX_BYTES];
+
+namespace {
+constexpr int kExportMaxDevices = 64;
+std::mutex g_export_mutex;
+void* g_export_addr[kExportMaxDevices] = {};  // device address of g_export_scratch
+}  // namespace
+
+extern "C" int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, double B0,
+                                           double rho0, double u0, void* solid, void* rho,
+                                           void* u) {
+  if (!h) return LBMPSM_ERR_ARG;
+  if (h->device < 0 || h->device >= kExportMaxDevices)
+    return fail(h, LBMPSM_ERR_ARG, "lbmpsm_export_fields_static: device index out of range");
+  const Geom& g = h->g;
+  const size_t npts = (size_t)(g.L[0] - 2) * (g.L[1] - 2) * (g.dim == 3 ? g.L[2] - 2 : 1);
+  const size_t es = as_double ? 8 : 4;
+  // only the requested fields are staged, packed solid | rho | u
+  const size_t b_solid = solid ? es * npts : 0, b_rho = rho ? es * npts : 0,
+               b_u = u ? 3 * es * npts : 0;
+  const size_t need = b_solid + b_rho + b_u;
+  if (need > (size_t)LBMPSM_EXPORT_STATIC_MAX_BYTES)
+    return fail(h, LBMPSM_ERR_CAPACITY,
+                "lbmpsm_export_fields_static: the requested fields of " + std::to_string(npts) +
+                    " nodes need " + std::to_string(need) +
+                    " bytes of scratch, more than its fixed " +
+                    std::to_string((size_t)LBMPSM_EXPORT_STATIC_MAX_BYTES) +
+                    "; request fewer fields, float output, or use lbmpsm_export_fields");
+  if (need == 0) return LBMPSM_OK;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  std::lock_guard<std::mutex> lock(g_export_mutex);
+  if (!g_export_addr[h->device]) {
+    void* a = nullptr;
+    CUDA_TRY(h, cudaGetSymbolAddress(&a, g_export_scratch));
+    g_export_addr[h->device] = a;
+  }
+  char* b = static_cast<char*>(g_export_addr[h->device]);
+  char* d_solid = solid ? b : nullptr;
+  char* d_rho = rho ? b + b_solid : nullptr;
+  char* d_u = u ? b + b_solid + b_rho : nullptr;
+  CUDA_TRY(h, launch_export_fields(g, h->tab, h->macro_valid ? h->rho : nullptr,
+                                   h->macro_valid ? h->u : nullptr, as_double, B0, rho0, u0,
+                                   d_solid, d_rho, d_u, h->stream));
+  if (solid) CUDA_TRY(h, cudaMemcpyAsync(solid, d_solid, b_solid, cudaMemcpyDeviceToHost, h->stream));
+  if (rho) CUDA_TRY(h, cudaMemcpyAsync(rho, d_rho, b_rho, cudaMemcpyDeviceToHost, h->stream));
+  if (u) CUDA_TRY(h, cudaMemcpyAsync(u, d_u, b_u, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return LBMPSM_OK;
+}

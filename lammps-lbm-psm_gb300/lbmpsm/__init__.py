@@ -37,7 +37,7 @@ SYMBOLS = (
     "lbmpsm_step", "lbmpsm_step_device", "lbmpsm_apply_bc", "lbmpsm_request_macro",
     "lbmpsm_export_fields", "lbmpsm_get_populations", "lbmpsm_set_populations",
     "lbmpsm_get_particle_table", "lbmpsm_check", "lbmpsm_synchronize", "lbmpsm_stream",
-    "lbmpsm_run_fixed", "lbmpsm_read_forces",
+    "lbmpsm_run_fixed", "lbmpsm_read_forces", "lbmpsm_export_fields_static",
 )
 
 
@@ -111,6 +111,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.lbmpsm_stream.restype = C.c_void_p
     lib.lbmpsm_run_fixed.argtypes = [H, C.c_int]
     lib.lbmpsm_read_forces.argtypes = [H, C.c_int, _D, _D, _D]
+    lib.lbmpsm_export_fields_static.argtypes = [H, C.c_int, C.c_double, C.c_double, C.c_double,
+                                                C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 
