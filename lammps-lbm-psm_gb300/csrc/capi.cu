@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -65,6 +66,7 @@ struct lbmpsm_handle {
   int last_n = 0;
   // graphs of one step for each parity (map + collide + reduce + bc)
   cudaGraphExec_t gexec[2]{nullptr, nullptr};
+  PipeConfig pipe{};  // launch shape of the FP32/FP16 collide kernel
   int graph_n = -1;
   int graph_bc = -1;
   size_t dev_bytes = 0;
@@ -320,6 +322,7 @@ int collide(lbmpsm_handle* h) {
   p.gpref_f = (float)p.guo_pref;
   p.tm_f = (float)(p.tau - 0.5);
   for (int d = 0; d < 3; ++d) p.F_f[d] = (float)p.F[d];
+  p.pipe = h->pipe;
   const int odd = (int)(h->t & 1);
   cudaError_t e;
   switch (h->opt.storage) {
@@ -600,6 +603,16 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
   cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream);
   if (launch_init_populations(g, h->f, o.storage, h->scale16, h->stream) != cudaSuccess)
     return bail(LBMPSM_ERR_CUDA);
+  if (o.storage != LBMPSM_STORAGE_FP64) {
+    // persistent row pipeline: stage count from LBMPSM_PIPE_STAGES (3, 4 or 5; default 3)
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess)
+      return bail(LBMPSM_ERR_CUDA);
+    const char* env = std::getenv("LBMPSM_PIPE_STAGES");
+    const int stages = env ? std::atoi(env) : 3;
+    if (prepare_collide_lowp(g, o.storage, sms, stages, &h->pipe) != cudaSuccess)
+      return bail(LBMPSM_ERR_CUDA);
+  }
   int rc = ensure_particles(h, std::max(o.max_images, 1), o.max_radius > 0 ? o.max_radius : 8.0 * h->dx);
   if (rc) {
     std::string m = h->err;

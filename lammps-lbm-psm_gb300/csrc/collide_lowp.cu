@@ -12,6 +12,8 @@
 // FP64 (particles.cu).
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "lbmpsm_internal.cuh"
 
 namespace lbmpsm {
@@ -33,125 +35,46 @@ struct Store<__half> {
   }
 };
 
-template <int cx, int cy, int cz>
-__device__ __forceinline__ float edotf(float vx, float vy, float vz) {
-  float s = 0.0f;
-  if (cx) s += cx > 0 ? vx : -vx;
-  if (cy) s += cy > 0 ? vy : -vy;
-  if (cz) s += cz > 0 ? vz : -vz;
-  return s;
+// e_q . v for compile-time components (folded once the q loop is unrolled;
+// -0 is the identity of IEEE addition, so the leading term costs nothing)
+__device__ __forceinline__ float sgn_add(float s, int c, float v) {
+  return c == 0 ? s : (c > 0 ? s + v : s - v);
+}
+__device__ __forceinline__ float edot(int cx, int cy, int cz, float vx, float vy, float vz) {
+  return sgn_add(sgn_add(sgn_add(-0.0f, cx, vx), cy, vy), cz, vz);
 }
 
-struct PsmNodeF {
-  bool has1, has2;
-  float B1, B2, omB;   // omB = (1 - Btot) * omega
-  float us1[3], us2[3];
-  float q1, q2;        // 1.5 |us|^2
-  float F1[3], F2[3];
-};
-
-// Guo forcing term (src/LBM_PSM_dynamics.h:102-116) in deviation form
-template <class L, int q>
-__device__ __forceinline__ float guo_f32(float ux, float uy, float uz, float eu, float gpref,
-                                         float Fx, float Fy, float Fz) {
-  constexpr int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
-  const float w = (float)L::w(q);
-  const float a = ((float)cx - ux) * Fx + ((float)cy - uy) * Fy + ((float)cz - uz) * Fz;
-  const float eF = edotf<cx, cy, cz>(Fx, Fy, Fz);
-  return gpref * w * (3.0f * a + 9.0f * eu * eF);
-}
-
-// PSM collision of direction q (src/LBM_PSM_BGK_dynamics.h:70-113)
-template <class L, int q, bool FORCE>
-__device__ __forceinline__ void collide_q_psm(float& gq, float drho, float rho, float ux,
-                                              float uy, float uz, float usq15, float omo,
-                                              float gpref, float Fx, float Fy, float Fz,
-                                              PsmNodeF& sn) {
-  constexpr int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
-  const float w = (float)L::w(q);
-  const float g = gq;
-  const float eu = edotf<cx, cy, cz>(ux, uy, uz);
-  const float geq = w * (drho + rho * (3.0f * eu + 4.5f * eu * eu - usq15));
-  const float Fq = FORCE ? guo_f32<L, q>(ux, uy, uz, eu, gpref, Fx, Fy, Fz) : 0.0f;
-  float sc1 = 0.0f, sc2 = 0.0f;
-  if (sn.has1) {
-    const float e1 = edotf<cx, cy, cz>(sn.us1[0], sn.us1[1], sn.us1[2]);
-    const float gs = w * (drho + rho * (3.0f * e1 + 4.5f * e1 * e1 - sn.q1));
-    sc1 = (gs - g) + omo * (g - geq);
-  }
-  if (sn.has2) {
-    const float e2 = edotf<cx, cy, cz>(sn.us2[0], sn.us2[1], sn.us2[2]);
-    const float gs = w * (drho + rho * (3.0f * e2 + 4.5f * e2 * e2 - sn.q2));
-    sc2 = (gs - g) + omo * (g - geq);
-  }
-  gq = g + sn.omB * (geq - g) + sn.B1 * sc1 + sn.B2 * sc2 + Fq;
-  if (sn.has1) {
-    const float t = -sn.B1 * sc1;
-    if (cx) sn.F1[0] += cx > 0 ? t : -t;
-    if (cy) sn.F1[1] += cy > 0 ? t : -t;
-    if (cz) sn.F1[2] += cz > 0 ? t : -t;
-  }
-  if (sn.has2) {
-    const float t = -sn.B2 * sc2;
-    if (cx) sn.F2[0] += cx > 0 ? t : -t;
-    if (cy) sn.F2[1] += cy > 0 ? t : -t;
-    if (cz) sn.F2[2] += cz > 0 ? t : -t;
-  }
-}
-
-template <class L, int q, bool FORCE>
-struct UnrollPsm {
-  __device__ __forceinline__ static void run(float* g, float drho, float rho, float ux, float uy,
-                                             float uz, float usq15, float omo, float gpref,
-                                             float Fx, float Fy, float Fz, PsmNodeF& sn) {
-    collide_q_psm<L, q, FORCE>(g[q], drho, rho, ux, uy, uz, usq15, omo, gpref, Fx, Fy, Fz, sn);
-    UnrollPsm<L, q + 1, FORCE>::run(g, drho, rho, ux, uy, uz, usq15, omo, gpref, Fx, Fy, Fz, sn);
-  }
-};
-template <class L, bool FORCE>
-struct UnrollPsm<L, L::Q, FORCE> {
-  __device__ __forceinline__ static void run(float*, float, float, float, float, float, float,
-                                             float, float, float, float, float, PsmNodeF&) {}
-};
-
-// plain BGK collision of every direction with the Guo term
-template <class L, int q, bool FORCE>
-struct UnrollFluid {
-  __device__ __forceinline__ static void run(float* g, float drho, float rho, float ux, float uy,
-                                             float uz, float usq15, float omega, float gpref,
-                                             float Fx, float Fy, float Fz) {
-    constexpr int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
-    const float w = (float)L::w(q);
-    const float eu = edotf<cx, cy, cz>(ux, uy, uz);
-    const float geq = w * (drho + rho * (3.0f * eu + 4.5f * eu * eu - usq15));
-    const float Fq = FORCE ? guo_f32<L, q>(ux, uy, uz, eu, gpref, Fx, Fy, Fz) : 0.0f;
-    g[q] = g[q] + omega * (geq - g[q]) + Fq;
-    UnrollFluid<L, q + 1, FORCE>::run(g, drho, rho, ux, uy, uz, usq15, omega, gpref, Fx, Fy, Fz);
-  }
-};
-template <class L, bool FORCE>
-struct UnrollFluid<L, L::Q, FORCE> {
-  __device__ __forceinline__ static void run(float*, float, float, float, float, float, float,
-                                             float, float, float, float, float) {}
-};
-
-// Collision of one node on its Q deviations f[], in place: macro values,
-// optional macro store, then either the plain BGK update (fluid node) or the
-// PSM solid operator with node forces.  flag / r1 / r2 are the node's table
-// entries, loaded by the caller.
+// Collision of one node on its Q deviations f[], in place
+// (src/LBM_PSM_BGK_dynamics.h:40-114, src/LBM_PSM_dynamics.h:43-116).
+//
+// With Omega_s^n = feq(rho, u_s^n) - f + (1 - omega)(f - feq) and
+// sum_n B_n = B_t the reference update
+//   f' = f + (1 - B_t) omega (feq - f) + sum_n B_n Omega_s^n + F_q
+// equals, term for term in exact arithmetic,
+//   f' = f + omega (feq - f) + F_q + sum_n B_n (feq(rho, u_s^n) - feq(rho, u)),
+// and the difference of the two equilibria of direction q is
+//   w_q rho [a (3 + 4.5 b) - 1.5 (|u_s|^2 - |u|^2)],  a = e.(u_s - u), b = e.(u_s + u),
+// which is how it is evaluated here (no cancellation between two O(w)
+// equilibria).  The node force of slot n, -B_n sum_q Omega_s^n e_q, is by the
+// moments of the D2Q9/D3Q19 equilibria (sum_q feq(rho, v) e_q = rho v)
+//   -B_n [rho u_s^n - j + omega F/2]       (j including the F/2 shift),
+// so it needs no per-direction accumulation.
+//
+// The warp takes the plain BGK loop when none of its nodes is a PSM node,
+// the one-slot loop when none holds two particles, else the two-slot loop;
+// an unused slot has B = 0 and leaves f' bit-identical to the shorter loop.
 template <class L, bool FORCE>
 __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const CollideParams& p,
                                                   long long n, uint8_t flag, float4 r1,
                                                   float4 r2) {
   constexpr int Q = L::Q;
-  float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+  float drho = -0.0f, jx = -0.0f, jy = -0.0f, jz = -0.0f;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
     drho += f[q];
-    if (cx) jx += cx > 0 ? f[q] : -f[q];
-    if (cy) jy += cy > 0 ? f[q] : -f[q];
-    if (cz) jz += cz > 0 ? f[q] : -f[q];
+    jx = sgn_add(jx, L::ex(q), f[q]);
+    jy = sgn_add(jy, L::ey(q), f[q]);
+    jz = sgn_add(jz, L::ez(q), f[q]);
   }
   const float Fx = p.F_f[0], Fy = p.F_f[1], Fz = p.F_f[2];
   if (FORCE) {
@@ -170,45 +93,80 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
   }
   const float usq15 = 1.5f * (ux * ux + uy * uy + uz * uz);
   const float omega = p.omega_f;
-  if (flag == 0) {
-    UnrollFluid<L, 0, FORCE>::run(f, drho, rho, ux, uy, uz, usq15, omega, p.gpref_f, Fx, Fy, Fz);
+  const float gpref = p.gpref_f;
+  const float uF = FORCE ? ux * Fx + uy * Fy + uz * Fz : 0.0f;
+  const float dr_u = drho - rho * usq15;
+
+  // BGK part of direction q: f + omega (feq - f) + F_q
+#define LBMPSM_BGK_Q(q)                                                              \
+  const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);                            \
+  const float w = (float)L::w(q);                                                   \
+  const float eu = edot(cx, cy, cz, ux, uy, uz);                                    \
+  const float geq = w * fmaf(rho * eu, fmaf(4.5f, eu, 3.0f), dr_u);                 \
+  float bgk = fmaf(omega, geq - f[q], f[q]);                                        \
+  if (FORCE) {                                                                      \
+    const float eF = edot(cx, cy, cz, Fx, Fy, Fz);                                  \
+    bgk += gpref * w * fmaf(9.0f * eu, eF, 3.0f * (eF - uF));                       \
+  }
+
+  const unsigned act = __activemask();
+  const bool psm = flag != 0;
+  if (!__any_sync(act, psm)) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      LBMPSM_BGK_Q(q)
+      f[q] = bgk;
+    }
     return;
   }
-  PsmNodeF sn;
-  sn.has1 = (flag & 1) != 0;
-  sn.has2 = (flag & 2) != 0;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) sn.F1[c] = sn.F2[c] = 0.0f;
-  float B1 = sn.has1 ? r1.x : 0.0f;
-  float B2 = sn.has2 ? r2.x : 0.0f;
+  const bool has1 = (flag & 1) != 0, has2 = (flag & 2) != 0;
+  float B1 = has1 ? r1.x : 0.0f;
+  float B2 = has2 ? r2.x : 0.0f;
   if (p.weighting == 1) {  // Noble-Torczynski weighting (opt-in)
     const float tm = p.tm_f;
-    if (sn.has1) B1 = B1 * tm / ((1.0f - B1) + tm);
-    if (sn.has2) B2 = B2 * tm / ((1.0f - B2) + tm);
+    if (has1) B1 = B1 * tm / ((1.0f - B1) + tm);
+    if (has2) B2 = B2 * tm / ((1.0f - B2) + tm);
   }
-  float Bt = B1 + B2;
+  const float Bt = B1 + B2;
   if (Bt > 1.0f) {
     B1 = B1 / Bt;
     B2 = B2 / Bt;
-    Bt = 1.0f;
   }
-  sn.B1 = B1;
-  sn.B2 = B2;
-  sn.omB = (1.0f - Bt) * omega;
-  sn.us1[0] = sn.has1 ? r1.y : 0.0f;
-  sn.us1[1] = sn.has1 ? r1.z : 0.0f;
-  sn.us1[2] = sn.has1 ? r1.w : 0.0f;
-  sn.us2[0] = sn.has2 ? r2.y : 0.0f;
-  sn.us2[1] = sn.has2 ? r2.z : 0.0f;
-  sn.us2[2] = sn.has2 ? r2.w : 0.0f;
-  sn.q1 = 1.5f * (sn.us1[0] * sn.us1[0] + sn.us1[1] * sn.us1[1] + sn.us1[2] * sn.us1[2]);
-  sn.q2 = 1.5f * (sn.us2[0] * sn.us2[0] + sn.us2[1] * sn.us2[1] + sn.us2[2] * sn.us2[2]);
-  UnrollPsm<L, 0, FORCE>::run(f, drho, rho, ux, uy, uz, usq15, p.omo_f, p.gpref_f, Fx, Fy, Fz, sn);
-  float* nf = static_cast<float*>(p.tab.nodeF) + 6 * n;
+  const float s1x = has1 ? r1.y : 0.0f, s1y = has1 ? r1.z : 0.0f, s1z = has1 ? r1.w : 0.0f;
+  const float s2x = has2 ? r2.y : 0.0f, s2y = has2 ? r2.z : 0.0f, s2z = has2 ? r2.w : 0.0f;
+  const float B1r = B1 * rho, B2r = B2 * rho;
+  const float dq1 = fmaf(1.5f, s1x * s1x + s1y * s1y + s1z * s1z, -usq15);
+  const float dq2 = fmaf(1.5f, s2x * s2x + s2y * s2y + s2z * s2z, -usq15);
+  if (!__any_sync(act, has2)) {
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    nf[c] = sn.F1[c];
-    nf[3 + c] = sn.F2[c];
+    for (int q = 0; q < Q; ++q) {
+      LBMPSM_BGK_Q(q)
+      const float a1 = edot(cx, cy, cz, s1x - ux, s1y - uy, s1z - uz);
+      const float b1 = edot(cx, cy, cz, s1x + ux, s1y + uy, s1z + uz);
+      f[q] = fmaf(B1r * w, fmaf(a1, fmaf(4.5f, b1, 3.0f), -dq1), bgk);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      LBMPSM_BGK_Q(q)
+      const float a1 = edot(cx, cy, cz, s1x - ux, s1y - uy, s1z - uz);
+      const float b1 = edot(cx, cy, cz, s1x + ux, s1y + uy, s1z + uz);
+      const float a2 = edot(cx, cy, cz, s2x - ux, s2y - uy, s2z - uz);
+      const float b2 = edot(cx, cy, cz, s2x + ux, s2y + uy, s2z + uz);
+      bgk = fmaf(B1r * w, fmaf(a1, fmaf(4.5f, b1, 3.0f), -dq1), bgk);
+      f[q] = fmaf(B2r * w, fmaf(a2, fmaf(4.5f, b2, 3.0f), -dq2), bgk);
+    }
+  }
+#undef LBMPSM_BGK_Q
+  if (psm) {
+    const float hx = 0.5f * omega * Fx, hy = 0.5f * omega * Fy, hz = 0.5f * omega * Fz;
+    float* nf = static_cast<float*>(p.tab.nodeF) + 6 * n;
+    nf[0] = -B1 * (fmaf(rho, s1x, -jx) + (FORCE ? hx : 0.0f));
+    nf[1] = -B1 * (fmaf(rho, s1y, -jy) + (FORCE ? hy : 0.0f));
+    nf[2] = -B1 * (fmaf(rho, s1z, -jz) + (FORCE ? hz : 0.0f));
+    nf[3] = -B2 * (fmaf(rho, s2x, -jx) + (FORCE ? hx : 0.0f));
+    nf[4] = -B2 * (fmaf(rho, s2y, -jy) + (FORCE ? hy : 0.0f));
+    nf[5] = -B2 * (fmaf(rho, s2z, -jz) + (FORCE ? hz : 0.0f));
   }
 }
 
@@ -304,6 +262,10 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_all() {
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
+// every bulk store group of this thread has finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read0() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
 __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -343,151 +305,327 @@ __device__ __forceinline__ unsigned row_mask(const Geom& g, int sy, int sz) {
 }
 __host__ __device__ constexpr int row_bit(int dy, int dz) { return (dy + 1) * 3 + (dz + 1); }
 
-// Staged variant: one block per x-row (sy, sz), one thread per node.  The Q
-// population rows the step reads are pulled into shared memory with one bulk
-// copy each, the x-shifts of streaming are applied as shared-memory index
-// offsets, and the Q output rows are pushed back with one bulk copy each.
+// next row of a block's sequence: rows r, r + G, r + 2G, ... with
+// G = dz * S1 + dy, kept as (sy, sz) without division
+__device__ __forceinline__ void next_row(int& sy, int& sz, int dy, int dz, int S1) {
+  sy += dy;
+  sz += dz;
+  if (sy >= S1) {
+    sy -= S1;
+    sz += 1;
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+// barrier over nthreads threads that also ANDs a predicate across them
+__device__ __forceinline__ bool named_bar_and(int id, int nthreads, bool v) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((int)v), "r"(id), "r"(nthreads)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase) {
+  for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+
+// Warp-specialised row pipeline of the collide / A-A stream step.  A
+// persistent grid; every block walks its x-rows r, r + G, r + 2G, ... through
+// NST shared-memory stages of Q population rows each.
+//   producer warp (the last warp): lane q moves direction q -- it stores the
+//     outputs of row k - NST from stage s once the consumers are done with
+//     it, waits until that store has read the stage, then loads the inputs of
+//     row k into it; so the loads run up to NST - 1 rows ahead.
+//   consumer warps: one thread per node of the row; wait for the stage,
+//     collide, write the outputs back into the stage in place, signal done.
 //   even step: own row, slot q in, slot opp(q) out;
 //   odd step : row -e_q, slot opp(q) in -> row +e_q, slot q out.
+// Within a row the x-shifts of streaming are shared-memory index offsets.
 // The A-A pattern makes each block the only reader and writer of the
-// locations it moves, so blocks need no synchronisation between them.
-template <class L, typename T, bool ODD, bool FORCE>
-__global__ void __launch_bounds__(STAGED_MAX_ROW, 4) collide_staged_kernel(CollideParams p) {
+// locations it moves, so blocks never wait for one another.  Every wait is
+// bounded: on expiry the block records STATUS_TIMEOUT, lets the copies it
+// issued land (bounded too) and returns.
+template <class L, typename T, bool ODD, bool FORCE, int NST, int MINB>
+__global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel(CollideParams p) {
+  static_assert(NST >= 2, "stages");
   constexpr int Q = L::Q;
+  static_assert(Q <= 32, "one producer lane per direction");
   extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long full[NST], done[NST];
   const Geom& g = p.g;
-  const int P0 = g.P0;
-  T* buf = reinterpret_cast<T*>(smem_raw);
-  const unsigned bar = smem_addr(smem_raw + (size_t)Q * P0 * sizeof(T));
+  const int P0 = g.P0, S0 = g.S[0], S1 = g.S[1];
+  const int R = S1 * g.S[2];
+  const int G = gridDim.x;
+  const int gdy = p.pipe.dy, gdz = p.pipe.dz;
+  const int ncons = (int)blockDim.x - 32;
   const unsigned row_bytes = (unsigned)(P0 * sizeof(T));
-  const int sy = blockIdx.x;
-  const int sz = blockIdx.y;
-  const long long own = ((long long)sz * g.S[1] + sy) * P0;
+  const unsigned stage_bytes = (unsigned)Q * row_bytes;
+  const unsigned smem0 = smem_addr(smem_raw);
   T* __restrict__ F = static_cast<T*>(p.f);
-  const long long Np = g.Np;
-  const float sc = p.scale16;
-  const unsigned rows = row_mask(g, sy, sz);
+  const int tid = threadIdx.x;
 
-  if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(smem_addr(&full[s]), 1);
+      mbar_init(smem_addr(&done[s]), (unsigned)ncons);
+    }
     fence_mbar_init();
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned bytes = 0;
+
+  if (tid >= ncons) {
+    // ------------------------------------------------------------ producer
+    const int lane = tid - ncons;
+    const bool mine = lane < Q;
+    int ey = 0, ez = 0, qo = 0;
 #pragma unroll
-    for (int q = 0; q < Q; ++q)
-      if (!ODD || ((rows >> row_bit(-L::ey(q), -L::ez(q))) & 1u)) bytes += row_bytes;
-    mbar_expect_tx(bar, bytes);
-    long long base;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      if (!ODD) {
-        bulk_load(smem_addr(buf + q * P0), F + q * Np + own, row_bytes, bar);
-      } else if (row_of(g, sy, sz, -L::ey(q), -L::ez(q), base)) {
-        bulk_load(smem_addr(buf + q * P0), F + L::opp(q) * Np + base, row_bytes, bar);
+    for (int qq = 0; qq < Q; ++qq)
+      if (qq == lane) {
+        ey = L::ey(qq);
+        ez = L::ez(qq);
+        qo = L::opp(qq);
+      }
+    const long long Np = g.Np;
+    int ly = blockIdx.x % S1, lz = blockIdx.x / S1;  // next row to load
+    int sy = ly, sz = lz;                            // next row to store
+    int ls = 0, lph = 0;                             // its stage and parity
+    int ss = 0, sph = 0;
+    int loaded = 0, stored = 0;
+    bool ok = true;
+    const int K = blockIdx.x < (unsigned)R ? (R - 1 - (int)blockIdx.x) / G + 1 : 0;
+    while (stored < K) {
+      const bool can_load = loaded < K && loaded - stored < NST;
+      if (!can_load) {
+        // store the oldest row once the consumers are done with it
+        // one decision for the whole warp (its lanes poll independently)
+        ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_addr(&done[ss]), sph));
+        if (!ok) break;
+        long long base = 0;
+        const bool ex = mine && (ODD ? row_of(g, sy, sz, ey, ez, base)
+                                     : (base = ((long long)sz * S1 + sy) * P0, true));
+        if (ex) bulk_store(F + lane * Np + base, smem0 + ss * stage_bytes + lane * row_bytes, row_bytes);
+        bulk_commit();
+        next_row(sy, sz, gdy, gdz, S1);
+        ++stored;
+        if (++ss == NST) {
+          ss = 0;
+          sph ^= 1;
+        }
+        continue;
+      }
+      if (loaded >= NST) {
+        // stage ls held row loaded - NST, stored just before: wait until the
+        // store has read it (each lane its own bulk group)
+        bulk_wait_read0();
+        __syncwarp();
+      }
+      long long base = 0;
+      const bool ex = mine && (ODD ? row_of(g, ly, lz, -ey, -ez, base)
+                                   : (base = ((long long)lz * S1 + ly) * P0, true));
+      const unsigned cnt = __popc(__ballot_sync(0xffffffffu, ex));
+      const unsigned bar = smem_addr(&full[ls]);
+      if (lane == 0) mbar_expect_tx(bar, cnt * row_bytes);
+      __syncwarp();
+      if (ex)
+        bulk_load(smem0 + ls * stage_bytes + lane * row_bytes, F + (ODD ? qo : lane) * Np + base,
+                  row_bytes, bar);
+      next_row(ly, lz, gdy, gdz, S1);
+      ++loaded;
+      if (++ls == NST) {
+        ls = 0;
+        lph ^= 1;
       }
     }
+    if (!ok) {
+      if (lane == 0) atomicOr(p.status, STATUS_TIMEOUT);
+      // let the loads still in flight land: rows stored .. loaded-1
+      int ts = ss, tph = sph;
+      for (int k = stored; k < loaded; ++k) {
+        mbar_wait_bounded(smem_addr(&full[ts]), tph);
+        if (++ts == NST) {
+          ts = 0;
+          tph ^= 1;
+        }
+      }
+    }
+    bulk_wait_all();
+    (void)lph;
+    return;
   }
-  // x neighbours of this thread's node (periodic wrap inside the row)
-  const int x = threadIdx.x;
-  const int S0 = g.S[0];
+
+  // -------------------------------------------------------------- consumers
+  const int x = tid;
   const bool active = x < S0;
   const int xm = x > 0 ? x - 1 : S0 - 1;
   const int xp = x < S0 - 1 ? x + 1 : 0;
   const bool vxm = x > 0 || g.per[0];
   const bool vxp = x < S0 - 1 || g.per[0];
-
-  // the node's particle-table entries, fetched while the bulk copies fly
-  const long long n = own + x;
-  uint8_t flag = 0;
-  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r1;
-  if (active) {
-    flag = p.tab.flag[n];
-    if (flag) {
-      r1 = p.tab.rec32[2 * n];
-      r2 = p.tab.rec32[2 * n + 1];
-    }
-  }
-  // one thread polls the mbarrier (bounded), the others wait at the block barrier
-  __shared__ int ready;
-  if (threadIdx.x == 0) {
-    int ok = 0;
-    for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it)
-      if (mbar_try_wait(bar, 0)) {
-        ok = 1;
-        break;
-      }
-    if (!ok) {
-      atomicOr(p.status, STATUS_TIMEOUT);
-      // let the copies already issued land before the block gives up its shared memory
-      for (long long it = 0; it < MBAR_SPIN_LIMIT && !mbar_try_wait(bar, 0); ++it) {
+  const float sc = p.scale16;
+  int cy = blockIdx.x % S1, cz = blockIdx.x / S1;
+  int s = 0, ph = 0;
+  for (int r = blockIdx.x; r < R; r += G) {
+    const long long own = ((long long)cz * S1 + cy) * P0;
+    const unsigned rows = row_mask(g, cy, cz);
+    constexpr unsigned need = L::Q == 9 ? 0x92u : 0x1FFu;  // (dy, dz) rows the set uses
+    const bool all_ok = (rows & need) == need && g.per[0];  // every source node exists
+    const long long n = own + x;
+    uint8_t flag = 0;
+    float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r1;
+    if (active) {
+      flag = p.tab.flag[n];
+      if (flag) {
+        r1 = p.tab.rec32[2 * n];
+        r2 = p.tab.rec32[2 * n + 1];
       }
     }
-    ready = ok;
-  }
-  __syncthreads();
-  if (!ready) return;
-
-  float f[Q];
-  if (active) {
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
-      // the source node x - e_q exists: row and x neighbour
-      const bool ok = ((rows >> row_bit(-cy, -cz)) & 1u) && (cx == 0 || (cx > 0 ? vxm : vxp));
-      const int xs = ODD ? (cx == 0 ? x : (cx > 0 ? xm : xp)) : x;
-      f[q] = ok ? Store<T>::load(buf + q * P0 + xs, sc) : 0.0f;
+    bool ok = true;
+    if (tid == 0) ok = mbar_wait_bounded(smem_addr(&full[s]), ph);
+    if (!named_bar_and(1, ncons, ok)) {
+      if (tid == 0) atomicOr(p.status, STATUS_TIMEOUT);
+      return;
     }
-    collide_node_lowp<L, FORCE>(f, p, n, flag, r1, r2);
-  }
-  __syncthreads();  // every input read before any output overwrites the rows
-  if (active) {
+    T* buf = reinterpret_cast<T*>(smem_raw + (size_t)s * stage_bytes);
+    float f[Q];
+    if (active) {
+      if (all_ok) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      if (!ODD) {
-        Store<T>::store(buf + L::opp(q) * P0 + x, f[q], sc);
+        for (int q = 0; q < Q; ++q) {
+          const int ex = L::ex(q);
+          const int xs = ODD ? (ex == 0 ? x : (ex > 0 ? xm : xp)) : x;
+          f[q] = Store<T>::load(buf + q * P0 + xs, sc);
+        }
       } else {
-        const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
-        const bool ok = ((rows >> row_bit(cy, cz)) & 1u) && (cx == 0 || (cx > 0 ? vxp : vxm));
-        const int xt = cx == 0 ? x : (cx > 0 ? xp : xm);
-        if (ok) Store<T>::store(buf + q * P0 + xt, f[q], sc);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int ex = L::ex(q), ey = L::ey(q), ez = L::ez(q);
+          // the source node x - e_q exists: row and x neighbour
+          const bool okq =
+              ((rows >> row_bit(-ey, -ez)) & 1u) && (ex == 0 || (ex > 0 ? vxm : vxp));
+          const int xs = ODD ? (ex == 0 ? x : (ex > 0 ? xm : xp)) : x;
+          f[q] = okq ? Store<T>::load(buf + q * P0 + xs, sc) : 0.0f;
+        }
       }
+      collide_node_lowp<L, FORCE>(f, p, n, flag, r1, r2);
+    }
+    // odd step: every input read before any output lands on a neighbour's
+    // column (the even step reads and writes only the thread's own column)
+    if (ODD) named_bar_sync(1, ncons);
+    if (active) {
+      if (!ODD) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) Store<T>::store(buf + L::opp(q) * P0 + x, f[q], sc);
+      } else if (all_ok) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int ex = L::ex(q);
+          const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
+          Store<T>::store(buf + q * P0 + xt, f[q], sc);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int ex = L::ex(q), ey = L::ey(q), ez = L::ez(q);
+          const bool okq = ((rows >> row_bit(ey, ez)) & 1u) && (ex == 0 || (ex > 0 ? vxp : vxm));
+          const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
+          if (okq) Store<T>::store(buf + q * P0 + xt, f[q], sc);
+        }
+      }
+    }
+    fence_async_smem();
+    mbar_arrive(smem_addr(&done[s]));
+    next_row(cy, cz, gdy, gdz, S1);
+    if (++s == NST) {
+      s = 0;
+      ph ^= 1;
     }
   }
-  fence_async_smem();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    long long base;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      if (!ODD) {
-        bulk_store(F + q * Np + own, smem_addr(buf + q * P0), row_bytes);
-      } else if (row_of(g, sy, sz, L::ey(q), L::ez(q), base)) {
-        bulk_store(F + q * Np + base, smem_addr(buf + q * P0), row_bytes);
-      }
-    }
-    bulk_commit();
-    bulk_wait_all();
+}
+
+template <class L, typename T, int NST, int MINB>
+static cudaError_t pipe_prepare(const Geom& g, int sm_count, PipeConfig* cfg) {
+  const int threads = (g.S[0] + 31) / 32 * 32 + 32;  // consumers + producer warp
+  const size_t smem = (size_t)NST * L::Q * g.P0 * sizeof(T);
+  cudaError_t e;
+  const void* fns[4] = {(const void*)collide_pipe_kernel<L, T, false, false, NST, MINB>,
+                        (const void*)collide_pipe_kernel<L, T, false, true, NST, MINB>,
+                        (const void*)collide_pipe_kernel<L, T, true, false, NST, MINB>,
+                        (const void*)collide_pipe_kernel<L, T, true, true, NST, MINB>};
+  for (const void* fn : fns)
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+      return e;
+  int per_sm = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[0], threads, smem)) !=
+      cudaSuccess)
+    return e;
+  if (per_sm < 1) return cudaSuccess;  // does not fit: direct kernel
+  const long long rows = (long long)g.S[1] * g.S[2];
+  const long long grid = std::min<long long>(rows, (long long)per_sm * sm_count);
+  cfg->stages = NST;
+  cfg->grid = (int)grid;
+  cfg->threads = threads;
+  cfg->smem = smem;
+  cfg->dy = (int)(grid % g.S[1]);
+  cfg->dz = (int)(grid / g.S[1]);
+  return cudaSuccess;
+}
+
+template <class L, typename T>
+static cudaError_t prepare_lowp(const Geom& g, int sm_count, int stages, PipeConfig* cfg) {
+  *cfg = PipeConfig{};
+  if (g.S[0] > STAGED_MAX_ROW) return cudaSuccess;
+  switch (stages) {
+    case 4: return pipe_prepare<L, T, 4, 2>(g, sm_count, cfg);
+    case 5: return pipe_prepare<L, T, 5, 2>(g, sm_count, cfg);
+    default: return pipe_prepare<L, T, 3, 3>(g, sm_count, cfg);
+  }
+}
+
+cudaError_t prepare_collide_lowp(const Geom& g, int storage, int sm_count, int stages,
+                                 PipeConfig* cfg) {
+  if (storage == 1)
+    return g.dim == 2 ? prepare_lowp<D2Q9, float>(g, sm_count, stages, cfg)
+                      : prepare_lowp<D3Q19, float>(g, sm_count, stages, cfg);
+  return g.dim == 2 ? prepare_lowp<D2Q9, __half>(g, sm_count, stages, cfg)
+                    : prepare_lowp<D3Q19, __half>(g, sm_count, stages, cfg);
+}
+
+template <class L, typename T, int NST, int MINB>
+static void launch_pipe(const CollideParams& p, int odd, cudaStream_t st) {
+  const PipeConfig& c = p.pipe;
+  if (odd) {
+    if (p.has_force)
+      collide_pipe_kernel<L, T, true, true, NST, MINB><<<c.grid, c.threads, c.smem, st>>>(p);
+    else
+      collide_pipe_kernel<L, T, true, false, NST, MINB><<<c.grid, c.threads, c.smem, st>>>(p);
+  } else {
+    if (p.has_force)
+      collide_pipe_kernel<L, T, false, true, NST, MINB><<<c.grid, c.threads, c.smem, st>>>(p);
+    else
+      collide_pipe_kernel<L, T, false, false, NST, MINB><<<c.grid, c.threads, c.smem, st>>>(p);
   }
 }
 
 template <class L, typename T>
 static cudaError_t launch_lowp(const CollideParams& p, int odd, cudaStream_t st) {
-  if (p.g.S[0] <= STAGED_MAX_ROW && p.g.S[2] <= 65535) {
-    const unsigned threads = (unsigned)((p.g.S[0] + 31) / 32 * 32);
-    const size_t smem = (size_t)L::Q * p.g.P0 * sizeof(T) + 16;
-    const dim3 rows((unsigned)p.g.S[1], (unsigned)p.g.S[2]);
-    if (odd) {
-      if (p.has_force)
-        collide_staged_kernel<L, T, true, true><<<rows, threads, smem, st>>>(p);
-      else
-        collide_staged_kernel<L, T, true, false><<<rows, threads, smem, st>>>(p);
-    } else {
-      if (p.has_force)
-        collide_staged_kernel<L, T, false, true><<<rows, threads, smem, st>>>(p);
-      else
-        collide_staged_kernel<L, T, false, false><<<rows, threads, smem, st>>>(p);
+  if (p.pipe.grid > 0) {
+    switch (p.pipe.stages) {
+      case 4: launch_pipe<L, T, 4, 2>(p, odd, st); break;
+      case 5: launch_pipe<L, T, 5, 2>(p, odd, st); break;
+      default: launch_pipe<L, T, 3, 3>(p, odd, st); break;
     }
     return cudaGetLastError();
   }

@@ -153,6 +153,14 @@ struct Table {
 };
 
 // ---------------------------------------------------------------- step params
+// launch shape of the row-pipelined FP32/FP16 collide kernel (grid 0: the
+// direct kernel instead)
+struct PipeConfig {
+  int grid = 0, threads = 0, stages = 0;
+  size_t smem = 0;
+  int dy = 0, dz = 0;  // grid = dz * S1 + dy
+};
+
 struct CollideParams {
   Geom g;
   void* f;                // populations (double / float / half)
@@ -170,6 +178,7 @@ struct CollideParams {
   // FP32 copies made on the host (double->float conversions are slow on the device)
   float omega_f, omo_f, gpref_f, tm_f;
   float F_f[3];
+  PipeConfig pipe;
 };
 
 // Exact small-integer to float conversion without the conversion unit:
@@ -294,6 +303,10 @@ enum : int { STATUS_LIST_OVERFLOW = 1, STATUS_NONFINITE = 2, STATUS_TIMEOUT = 4 
 cudaError_t launch_collide_f64(const CollideParams& p, int odd, cudaStream_t st);
 cudaError_t launch_collide_f32(const CollideParams& p, int odd, cudaStream_t st);
 cudaError_t launch_collide_f16(const CollideParams& p, int odd, cudaStream_t st);
+// storage 1 (FP32) or 2 (FP16); sets the kernels' shared-memory limit and
+// sizes the persistent grid from the occupancy on this device
+cudaError_t prepare_collide_lowp(const Geom& g, int storage, int sm_count, int stages,
+                                 PipeConfig* cfg);
 cudaError_t launch_bc_f64(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f32(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f16(const BCParams& p, cudaStream_t st);
