@@ -45,6 +45,7 @@ TAU = 0.65
 U_WALL = 0.01
 SEED = 20261203
 METRIC = "D3Q19 PSM MLUPS & % HBM roofline, FP32 vs FP64 at fixed drag error, 1 GB300"
+REF_MAX_STEPS = 20
 BYTES_PER_NODE = {"fp64": 2 * 19 * 8, "fp32": 2 * 19 * 4, "fp16": 2 * 19 * 2}
 
 
@@ -98,7 +99,8 @@ def images(edge=None, nspheres=None):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms; only the
+    samples that arrive inside the marked timed window are summarised."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -107,26 +109,34 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
+        self.window = (0.0, 0.0)
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.monotonic()
+            while not self.lines and time.monotonic() - t0 < 3.0:  # sampler is running
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def mark(self, start: float, end: float):
+        self.window = (start, end)
 
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.06)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -136,7 +146,10 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        t0, t1 = self.window
+        for ts, ln in self.lines:
+            if not (t0 <= ts <= t1 + 0.06):
+                continue
             p = [s.strip() for s in ln.split(",")]
             if len(p) < 9:
                 continue
@@ -207,18 +220,38 @@ def run_ours(args, rank=0, world=1):
         return e0.elapsed_time(e1) / 1e3
 
     K, W = args.steps, args.warmup
+    from lbmpsm.host import reverse_comm
+
+    def owner_forces(lt):
+        """F, T, S of the local particles after the ghost images' partial
+        sums are added into their owners (CommBrick::reverse_comm)."""
+        parts = lt.read_forces(n)
+        return [reverse_comm(a, g.owner, g.swap, nloc)[:nloc] for a in parts]
+
+    def accuracy_point(lt):
+        """One more host step with the macro fields requested: forces and the
+        velocity field after 2 + W + K steps."""
+        lt.request_macro()
+        lt.step(g.tag, g.x, g.v, g.omega, g.radius)
+        lt.apply_bc()
+        fts = owner_forces(lt)
+        u = lt.export_fields(1.0, 1.0, 1.0, as_double=True)[2]
+        return fts, u
+
     # FP32 storage: the headline path
     lat = make(args.storage)
     lat.step(g.tag, g.x, g.v, g.omega, g.radius)  # images go up once, map + step
     lat.apply_bc()
-    lat.run_fixed(W)
-    lat.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
     with ClockSampler(device) as clk:
+        lat.run_fixed(W)
+        lat.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t_a = time.monotonic()
         t_val = ev_time(lat, lambda: lat.run_fixed(K))
+        clk.mark(t_a, time.monotonic())
     t_val = max_over_ranks(t_val, world)
-    f32_forces = lat.read_forces(nloc)[0]
+    acc32 = accuracy_point(lat)
 
     # end to end: host arrays through lbmpsm_step, copies every step
     t0 = time.perf_counter()
@@ -228,7 +261,8 @@ def run_ours(args, rank=0, world=1):
     lat.synchronize()
     t_e2e = max_over_ranks(time.perf_counter() - t0, world)
 
-    # the collide-stream kernel alone (lattice-only steps, particle table in place)
+    # the collide-stream kernel alone: lattice-only steps (no images, so the
+    # step launches only the collide kernel; the particle table stays in place)
     def lattice_only(lt, steps):
         def go():
             for _ in range(steps):
@@ -237,29 +271,42 @@ def run_ours(args, rank=0, world=1):
     t_kernel = ev_time(lat, lattice_only(lat, K)) / K
     lat.close()
 
-    # plain FP64 path on the same workload
+    # plain FP64 path on the same workload, same step count at the accuracy point
     fp64 = None
-    drag_err = None
+    accuracy = None
     if not args.no_fp64:
         lat64 = make("fp64")
         lat64.step(g.tag, g.x, g.v, g.omega, g.radius)
         lat64.apply_bc()
-        K64 = max(3, K // 4)
-        lat64.run_fixed(max(0, W + K - K64))  # same step count as the FP32 forces above
+        K64 = max(3, K // 8)
+        lat64.run_fixed(max(0, W + K - K64))
         lat64.synchronize()
         t64 = ev_time(lat64, lambda: lat64.run_fixed(K64))
-        f64_forces = lat64.read_forces(nloc)[0]
+        acc64 = accuracy_point(lat64)
         t64_kernel = ev_time(lat64, lattice_only(lat64, 3)) / 3
         lat64.close()
         mlups64 = nodes * K64 / t64 / 1e6
-        drag_err = float(np.abs(f32_forces - f64_forces).max() / np.abs(f64_forces).max())
         fp64 = (mlups64, t64_kernel)
+
+        def rel(a, b):
+            return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+        (F32, T32, S32), u32 = acc32
+        (F64, T64, S64), u64 = acc64
+        accuracy = {
+            "vs": "FP64 GPU path (bit-identical to the CPU oracle on the parity cases)",
+            "step": 2 + W + K,
+            "drag": rel(F32, F64), "torque": rel(T32, T64), "stresslet": rel(S32, S64),
+            "velocity_l2": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+            "velocity_max": rel(u32, u64),
+            "metric": "max |x32 - x64| / max |x64| over particles (F, T, S) or nodes (u)",
+        }
 
     mlups = nodes * K * world / t_val / 1e6
     peak, peak_kind = measured_peak_gbs()
     achieved = BYTES_PER_NODE[args.storage] * nodes / t_kernel / 1e9
     traffic = profile_traffic()
-    launches_per_step = 8  # map: prep, scan, fill, sort, apply; collide; reduce; bc
+    # map: prep, scan, fill, sort, solid fraction, apply; collide; reduce; bc
+    launches_per_step = 9
     out = {
         "metric": METRIC,
         "value": round(mlups, 1),
@@ -284,14 +331,16 @@ def run_ours(args, rank=0, world=1):
                 "h2d_bytes_per_step": int(n * (4 + 10 * 8)), "d2h_bytes_per_step": int(n * 12 * 8)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": f"collide_lowp_kernel<D3Q19,{'float' if args.storage == 'fp32' else '__half'}> (A-A, even/odd)",
-                     "algorithmic_bytes_per_node": BYTES_PER_NODE["fp32"],
+                     "kernel": f"collide_pipe_kernel<D3Q19,{'float' if args.storage == 'fp32' else '__half'}> "
+                               "(warp-specialised row pipeline, A-A even/odd)",
+                     "algorithmic_bytes_per_node": BYTES_PER_NODE[args.storage],
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
         "fp64_plain": None if fp64 is None else {
             "value": round(fp64[0], 1), "unit": "MLUPS", "kernel_ms": round(fp64[1] * 1e3, 3),
             "hbm_frac": round(BYTES_PER_NODE["fp64"] * nodes / fp64[1] / 1e9 / peak, 4)},
         "fp32_over_fp64": None if fp64 is None else round(mlups / world / fp64[0], 2),
-        "drag_rel_err_fp32_vs_fp64": drag_err,
+        "drag_rel_err_fp32_vs_fp64": None if accuracy is None else accuracy["drag"],
+        "accuracy_fp32_vs_fp64": accuracy,
         "kernel_ms": round(t_kernel * 1e3, 4),
         "gpu_launches": launches_per_step * K,
         "clocks": clk.summary(),
@@ -340,12 +389,15 @@ def cpu_baseline(steps, threads=None):
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    cb = cpu_baseline(max(1, args.steps))
+    # a full 256^3 coupling step takes ~1.3 s on 16 Grace cores: time at most
+    # REF_MAX_STEPS of them so that the run ends within a minute or so
+    steps = min(max(1, args.steps), REF_MAX_STEPS)
+    cb = cpu_baseline(steps)
     nodes = EDGE ** 3
     return {
         "metric": METRIC, "value": cb["value"], "unit": "MLUPS", "n_gpus": world,
-        "steps": max(1, args.steps), "warmup": 1,
-        "ms_per_step": round(cb["seconds"] / max(1, args.steps) * 1e3, 1),
+        "steps": steps, "warmup": 1,
+        "ms_per_step": round(cb["seconds"] / steps * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
         "config": {"workload": "sheared suspension: D3Q19 256^3, y Zou-He shear walls +-0.01, "
@@ -360,7 +412,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-steps", type=int, default=3)

@@ -165,7 +165,7 @@ int lbmpsm_export_fields(lbmpsm_handle* h, int as_double, double B0, double rho0
 
 /* Post-stream populations in the reference layout (local array with halo,
  * f[node*q+iq], FP64).  Replaces LBMPSMLattice::getVector_f_curr /
- * setVector_f_curr (src/LBM_PSM_lattice.cpp:230-232) as used by
+ * setVector_f_curr (src/LBM_PSM_lattice.cpp:250-252) as used by
  * `fix lbm-psm-restart` (src/fix_LBM_PSM_writeReadRestart.cpp:62,75).
  * Halo planes of periodic axes are returned as copies of the periodic twin
  * and ignored on input. */
