@@ -57,7 +57,9 @@ struct lbmpsm_handle {
   int* d_list = nullptr;
   unsigned short* d_sfcode = nullptr;  // solid-fraction codes of (image, box node) pairs
   long long sf_cap = 0;
-  unsigned long long* d_pair_total = nullptr;  // [0] list pairs, [1] codes
+  unsigned long long* d_pair_total = nullptr;  // [0] list pairs, [1] codes, [2] shell nodes
+  int4* d_shell = nullptr;  // shell nodes of the solid-fraction map (sf_cap entries)
+  int sm_count = 1;
   int* d_status = nullptr;
   double* d_check = nullptr;
   double* d_sf_value = nullptr;  // n/10^d for n = 0..1000
@@ -223,7 +225,9 @@ void free_particles(lbmpsm_handle* h) {
   dfree(h->d_img);
   dfree(h->d_list);
   dfree(h->d_sfcode);
+  dfree(h->d_shell);
   h->d_sfcode = nullptr;
+  h->d_shell = nullptr;
   h->sf_cap = 0;
   h->d_tag = nullptr;
   h->d_xvw = nullptr;
@@ -290,9 +294,12 @@ int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
   if (need_sf > h->sf_cap) {
     drop_graphs(h);
     dfree(h->d_sfcode);
+    dfree(h->d_shell);
     h->d_sfcode = nullptr;
+    h->d_shell = nullptr;
     long long cap = std::max(need_sf, 2 * h->sf_cap);
     CUDA_TRY(h, dmalloc(h, &h->d_sfcode, sizeof(unsigned short) * (size_t)cap));
+    CUDA_TRY(h, dmalloc(h, &h->d_shell, sizeof(int4) * (size_t)cap));
     h->sf_cap = cap;
   }
   return LBMPSM_OK;
@@ -350,7 +357,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
   if (n > 0) {
     const int ncells = h->C[0] * h->C[1] * h->C[2];
     CUDA_TRY(h, cudaMemsetAsync(h->d_cells, 0, sizeof(int) * 3 * (size_t)ncells, h->stream));
-    CUDA_TRY(h, cudaMemsetAsync(h->d_pair_total, 0, 2 * sizeof(unsigned long long), h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_pair_total, 0, 4 * sizeof(unsigned long long), h->stream));
     MapParams m{};
     m.g = h->g;
     m.tab = h->tab;
@@ -381,6 +388,9 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     m.sfcode = h->d_sfcode;
     m.sf_cap = h->sf_cap;
     m.sf_value = h->d_sf_value;
+    m.shell = h->d_shell;
+    m.shell_cap = h->sf_cap;
+    m.sm_count = h->sm_count;
     m.status = h->d_status;
     m.write32 = h->opt.storage != LBMPSM_STORAGE_FP64 ? 1 : 0;
     CUDA_TRY(h, launch_map(m, h->stream));
@@ -389,6 +399,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
   if (rc) return rc;
   if (n > 0) {
     ReduceParams rp{};
+    rp.img = h->d_img;
     rp.g = h->g;
     rp.tab = h->tab;
     rp.n = n;
@@ -579,7 +590,7 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
     return bail(LBMPSM_ERR_NOMEM);
   const int ncells = h->C[0] * h->C[1] * h->C[2];
   if (dmalloc(h, &h->d_cells, sizeof(int) * 3 * (size_t)ncells) != cudaSuccess ||
-      dmalloc(h, &h->d_pair_total, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      dmalloc(h, &h->d_pair_total, 4 * sizeof(unsigned long long)) != cudaSuccess ||
       dmalloc(h, &h->d_status, sizeof(int)) != cudaSuccess ||
       dmalloc(h, &h->d_check, sizeof(double) * (4 + 4 * 1024)) != cudaSuccess ||
       dmalloc(h, &h->d_sf_value, sizeof(double) * 1001) != cudaSuccess)
@@ -603,11 +614,12 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
   cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream);
   if (launch_init_populations(g, h->f, o.storage, h->scale16, h->stream) != cudaSuccess)
     return bail(LBMPSM_ERR_CUDA);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess)
+    return bail(LBMPSM_ERR_CUDA);
+  h->sm_count = std::max(sms, 1);
   if (o.storage != LBMPSM_STORAGE_FP64) {
     // persistent row pipeline: stage count from LBMPSM_PIPE_STAGES (3, 4 or 5; default 3)
-    int sms = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess)
-      return bail(LBMPSM_ERR_CUDA);
     const char* env = std::getenv("LBMPSM_PIPE_STAGES");
     const int stages = env ? std::atoi(env) : 3;
     if (prepare_collide_lowp(g, o.storage, sms, stages, &h->pipe) != cudaSuccess)

@@ -245,6 +245,7 @@ struct Img {
   int has_spin;       // any omega component non-zero
   long long sf_off;   // offset of this image's box in the solid-fraction code scratch
   int box[3];         // box extents (hi - lo)
+  int rlo[3], rhi[3]; // force-reduction box, reference frame, clamped to interior nodes
 };
 
 // Solid-fraction codes of one (image, node) pair: 0..1000 = number of
@@ -271,10 +272,13 @@ struct MapParams {
   int* cell_fill;
   int* list;
   long long list_cap;
-  unsigned long long* pair_total;  // [0] cell-list pairs, [1] solid-fraction codes
+  unsigned long long* pair_total;  // [0] cell-list pairs, [1] solid-fraction codes, [2] shell nodes
   unsigned short* sfcode;          // codes of all (image, box node) pairs
   long long sf_cap;
   const double* sf_value;          // sf_value[n] = n/10^d (n = 0..1000), FP64
+  int4* shell;                     // shell nodes: image, box index, x | y << 16, z
+  long long shell_cap;
+  int sm_count;                    // multiprocessors (persistent grids)
   int* status;
   int write32;        // also write the FP32 mirror
 };
@@ -282,6 +286,7 @@ struct MapParams {
 struct ReduceParams {
   Geom g;
   Table tab;
+  const Img* img;     // image records of the step's map (centre, box)
   int n;
   const int* tag;
   const double* x;

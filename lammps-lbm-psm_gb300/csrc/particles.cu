@@ -37,43 +37,79 @@ static __device__ __forceinline__ double local_centre(double x, double origin, d
   return g - ((0 - ((double)0 * 2.0 * (double)1)) - 1);
 }
 
-__global__ void img_prep_kernel(MapParams p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
-  const Geom& g = p.g;
-  Img im;
-  im.tag = p.tag[i];
-  const double r = p.radius[i] / p.dx;
-  im.r = r;
-  bool valid = true;
+// Box of one image for the force reduction, clamped to interior nodes
+// (src/LBM_PSM_exchangeParticleData.cpp:188-195).
+static __device__ __forceinline__ void reduce_box_of(const Geom& g, const double xl[3], double r,
+                                                     int lo[3], int hi[3]) {
   for (int d = 0; d < 3; ++d) {
-    const double xl = local_centre(p.x[3 * i + d], p.origin[d], p.dx);
-    im.xl[d] = xl;
-    int lo = (int)(xl - r) - 2;
-    int hi = (int)(xl + r) + 2;
-    lo = clampi(lo, 0, g.L[d]);
-    hi = clampi(hi, 0, g.L[d]);
-    if (d == 2) {  // 2-D keeps its single z layer
-      if (lo < 0) lo = 0;
-      if (hi < 1) hi = 1;
-    }
-    // reference halo frame -> device storage
-    int slo, shi;
-    if (g.off[d] == 1) {
-      slo = (lo < 1 ? 1 : lo) - 1;
-      shi = (hi > g.L[d] - 1 ? g.L[d] - 1 : hi) - 1;
+    int a = (int)(xl[d] - r) - 2;
+    int c = (int)(xl[d] + r) + 2;
+    if (d < 2 || g.dim == 3) {
+      a = clampi(a, 1, g.L[d] - 1);
+      c = clampi(c, 1, g.L[d] - 1);
+      if (d == 2) {
+        if (a < 0) a = 0;
+        if (c < 1) c = 1;
+      }
     } else {
-      slo = lo;
-      shi = hi;
+      // fmax(fmin(fmax(z, 1), nz - 1), slot) with nz = 1 in 2-D
+      a = a < 1 ? 1 : a;
+      a = a > g.L[2] - 1 ? g.L[2] - 1 : a;
+      a = a < 0 ? 0 : a;
+      c = c < 1 ? 1 : c;
+      c = c > g.L[2] - 1 ? g.L[2] - 1 : c;
+      c = c < 1 ? 1 : c;
     }
-    im.lo[d] = slo;
-    im.hi[d] = shi;
-    if (slo >= shi) valid = false;
-    im.uT[d] = p.v[3 * i + d] / p.Uc * p.u_lb;
-    im.om[d] = p.omega[3 * i + d] * p.tc * p.dt_d;
+    lo[d] = a;
+    hi[d] = c;
   }
-  im.valid = valid;
-  {
+}
+
+// One thread per image builds its record (the FP64 arithmetic of
+// src/LBM_PSM_exchangeParticleData.cpp:31-55); then the warp counts its 32
+// images into the cells their boxes touch, one image at a time with the
+// lanes spread over the image's cells, and reserves the images' ranges of
+// solid-fraction codes with one atomic per warp.
+__global__ void img_prep_kernel(MapParams p) {
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool mine = i < p.n;
+  int cr[6] = {0, 0, 0, -1, -1, -1};  // clo[3], chi[3]
+  unsigned long long vol = 0;
+  Img im;
+  if (mine) {
+    const Geom& g = p.g;
+    im.tag = p.tag[i];
+    const double r = p.radius[i] / p.dx;
+    im.r = r;
+    bool valid = true;
+    for (int d = 0; d < 3; ++d) {
+      const double xl = local_centre(p.x[3 * i + d], p.origin[d], p.dx);
+      im.xl[d] = xl;
+      int lo = (int)(xl - r) - 2;
+      int hi = (int)(xl + r) + 2;
+      lo = clampi(lo, 0, g.L[d]);
+      hi = clampi(hi, 0, g.L[d]);
+      if (d == 2) {  // 2-D keeps its single z layer
+        if (lo < 0) lo = 0;
+        if (hi < 1) hi = 1;
+      }
+      // reference halo frame -> device storage
+      int slo, shi;
+      if (g.off[d] == 1) {
+        slo = (lo < 1 ? 1 : lo) - 1;
+        shi = (hi > g.L[d] - 1 ? g.L[d] - 1 : hi) - 1;
+      } else {
+        slo = lo;
+        shi = hi;
+      }
+      im.lo[d] = slo;
+      im.hi[d] = shi;
+      if (slo >= shi) valid = false;
+      im.uT[d] = p.v[3 * i + d] / p.Uc * p.u_lb;
+      im.om[d] = p.omega[3 * i + d] * p.tc * p.dt_d;
+    }
+    im.valid = valid;
     const double rP = r + p.sqrt2half;
     const double rM = r - p.sqrt2half;
     im.rP2 = rP * rP;
@@ -98,73 +134,122 @@ __global__ void img_prep_kernel(MapParams p) {
       if (__double_as_longlong(im.uT[d]) == (long long)0x8000000000000000ull) plain = false;
     }
     im.has_spin = plain ? 0 : 1;
-  }
-  im.sf_off = 0;
-  for (int d = 0; d < 3; ++d) im.box[d] = valid ? im.hi[d] - im.lo[d] : 0;
-  if (valid) {
-    const unsigned long long vol = (unsigned long long)im.box[0] * im.box[1] * im.box[2];
-    im.sf_off = (long long)atomicAdd(&p.pair_total[1], vol);
-  }
-  long long ncell = 0;
-  if (valid) {
-    for (int d = 0; d < 3; ++d) {
-      im.clo[d] = im.lo[d] / p.cb[d];
-      im.chi[d] = (im.hi[d] - 1) / p.cb[d];
+    reduce_box_of(g, im.xl, r, im.rlo, im.rhi);
+    for (int d = 0; d < 3; ++d) im.box[d] = valid ? im.hi[d] - im.lo[d] : 0;
+    if (valid) {
+      vol = (unsigned long long)im.box[0] * im.box[1] * im.box[2];
+      for (int d = 0; d < 3; ++d) {
+        im.clo[d] = im.lo[d] / p.cb[d];
+        im.chi[d] = (im.hi[d] - 1) / p.cb[d];
+        cr[d] = im.clo[d];
+        cr[3 + d] = im.chi[d];
+      }
+    } else {
+      for (int d = 0; d < 3; ++d) im.clo[d] = 0, im.chi[d] = -1;
     }
-    ncell = (long long)(im.chi[0] - im.clo[0] + 1) * (im.chi[1] - im.clo[1] + 1) *
-            (im.chi[2] - im.clo[2] + 1);
-    for (int cz = im.clo[2]; cz <= im.chi[2]; ++cz)
-      for (int cy = im.clo[1]; cy <= im.chi[1]; ++cy)
-        for (int cx = im.clo[0]; cx <= im.chi[0]; ++cx)
-          atomicAdd(&p.cell_count[(cz * p.C[1] + cy) * p.C[0] + cx], 1);
-    atomicAdd(&p.pair_total[0], (unsigned long long)ncell);
-  } else {
-    for (int d = 0; d < 3; ++d) im.clo[d] = 0, im.chi[d] = -1;
   }
-  p.img[i] = im;
+  // code ranges: warp prefix of the box volumes, one atomic per warp
+  unsigned long long incl = vol;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += x;
+  }
+  unsigned long long base = 0;
+  if (lane == 31) base = atomicAdd(&p.pair_total[1], incl);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  if (mine) {
+    im.sf_off = (long long)(base + incl - vol);
+    p.img[i] = im;
+  }
+  // cell counts, one image of the warp at a time
+  unsigned long long pairs = 0;
+  for (int j = 0; j < 32; ++j) {
+    int c[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) c[k] = __shfl_sync(0xffffffffu, cr[k], j);
+    const int nx = c[3] - c[0] + 1, ny = c[4] - c[1] + 1, nz = c[5] - c[2] + 1;
+    if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
+    const int ncell = nx * ny * nz;
+    pairs += (unsigned long long)ncell;
+    for (int t = lane; t < ncell; t += 32) {
+      const int cx = c[0] + t % nx, cy = c[1] + (t / nx) % ny, cz = c[2] + t / (nx * ny);
+      atomicAdd(&p.cell_count[(cz * p.C[1] + cy) * p.C[0] + cx], 1);
+    }
+  }
+  if (lane == 0 && pairs) atomicAdd(&p.pair_total[0], pairs);
 }
 
-// Exclusive scan of the cell counts, one block of 1024 threads.
-__global__ void cell_scan_kernel(const int* __restrict__ count, int* __restrict__ off,
-                                 int ncells) {
-  __shared__ long long part[1024];
-  const int t = threadIdx.x;
-  const int chunk = (ncells + 1023) / 1024;
-  const int b = t * chunk, e = min(ncells, b + chunk);
-  long long s = 0;
-  for (int c = b; c < e; ++c) s += count[c];
-  part[t] = s;
+// Exclusive scan of the cell counts: one block of 1024 threads walking tiles
+// of 4096 counts (4 consecutive per thread), warp shuffles within a tile and
+// a running carry between tiles.
+constexpr int SCAN_THREADS = 1024;
+__global__ void __launch_bounds__(SCAN_THREADS) cell_scan_kernel(const int* __restrict__ count,
+                                                                 int* __restrict__ off,
+                                                                 int ncells) {
+  __shared__ int wsum[SCAN_THREADS / 32];
+  __shared__ int carry_s;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0) carry_s = 0;
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    long long v = t >= o ? part[t - o] : 0;
+  for (int base = 0; base < ncells; base += 4 * SCAN_THREADS) {
+    const int i0 = base + 4 * t;
+    int v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = i0 + k < ncells ? count[i0 + k] : 0;
+    const int own = v[0] + v[1] + v[2] + v[3];
+    int incl = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int x = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += x;
+    }
+    if (lane == 31) wsum[warp] = incl;
     __syncthreads();
-    part[t] += v;
+    if (warp == 0) {
+      int w = wsum[lane];
+      int wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, wi, o);
+        if (lane >= o) wi += x;
+      }
+      wsum[lane] = wi - w;  // exclusive prefix of the warps
+    }
     __syncthreads();
-  }
-  long long run = part[t] - s;  // exclusive prefix of this chunk
-  for (int c = b; c < e; ++c) {
-    off[c] = (int)run;
-    run += count[c];
+    int run = carry_s + wsum[warp] + incl - own;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (i0 + k < ncells) off[i0 + k] = run;
+      run += v[k];
+    }
+    __syncthreads();
+    if (t == SCAN_THREADS - 1) carry_s = run;
+    __syncthreads();
   }
 }
 
+// One warp per image: the lanes enter the image into its cells' lists.
 __global__ void img_fill_kernel(MapParams p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (i >= p.n) return;
   if (p.pair_total[0] > (unsigned long long)p.list_cap ||
       p.pair_total[1] > (unsigned long long)p.sf_cap) {
-    if (i == 0) atomicOr(p.status, STATUS_LIST_OVERFLOW);
+    if (i == 0 && lane == 0) atomicOr(p.status, STATUS_LIST_OVERFLOW);
     return;
   }
   const Img& im = p.img[i];
   if (!im.valid) return;
-  for (int cz = im.clo[2]; cz <= im.chi[2]; ++cz)
-    for (int cy = im.clo[1]; cy <= im.chi[1]; ++cy)
-      for (int cx = im.clo[0]; cx <= im.chi[0]; ++cx) {
-        const int c = (cz * p.C[1] + cy) * p.C[0] + cx;
-        const int pos = atomicAdd(&p.cell_fill[c], 1);
-        p.list[(long long)p.cell_off[c] + pos] = i;
-      }
+  const int nx = im.chi[0] - im.clo[0] + 1, ny = im.chi[1] - im.clo[1] + 1,
+            nz = im.chi[2] - im.clo[2] + 1;
+  const int ncell = nx * ny * nz;
+  for (int t = lane; t < ncell; t += 32) {
+    const int cx = im.clo[0] + t % nx, cy = im.clo[1] + (t / nx) % ny, cz = im.clo[2] + t / (nx * ny);
+    const int c = (cz * p.C[1] + cy) * p.C[0] + cx;
+    const int pos = atomicAdd(&p.cell_fill[c], 1);
+    p.list[(long long)p.cell_off[c] + pos] = i;
+  }
 }
 
 __global__ void cell_sort_kernel(MapParams p, int ncells) {
@@ -182,44 +267,6 @@ __global__ void cell_sort_kernel(MapParams p, int ncells) {
     }
     a[j + 1] = v;
   }
-}
-
-// calcSolidFraction (src/LBM_PSM_exchangeParticleData.cpp:116-169): the
-// sub-cell count evaluated exactly in FP64 with the reference's expressions,
-// split over the 8 lanes of a group (lane `sub` takes the (a, b) rows sub,
-// sub+8, ...).  All 32 lanes of the warp must call it (shuffles); lanes of
-// groups without work pass valid = false.  Used whenever an FP32 decision
-// cannot be proven equal to the reference's.
-static __device__ int subcell_count_exact_group8(bool valid, int dim, double dx, double dy,
-                                                 double dz, double rP_LB, int sub) {
-  int n = 0;
-  if (valid) {
-    const double sliceWidth = 1.0 / ((double)10);
-    const double rSq = rP_LB * rP_LB;
-    double az[10];
-#pragma unroll
-    for (int c = 0; c < 10; ++c) {
-      const double delta = -0.5 + ((double)c + 0.5) * sliceWidth;
-      const double dzi = dz + delta;
-      az[c] = dzi * dzi;
-    }
-    for (int r = sub; r < 100; r += 8) {
-      const int a = r / 10, b = r % 10;
-      const double da = dx + (-0.5 + ((double)a + 0.5) * sliceWidth);
-      const double db = dy + (-0.5 + ((double)b + 0.5) * sliceWidth);
-      const double ax = da * da, ay = db * db;
-      if (dim == 2) {
-        if (ax + ay < rSq) ++n;
-      } else {
-#pragma unroll
-        for (int c = 0; c < 10; ++c)
-          if (ax + ay + az[c] < rSq) ++n;
-      }
-    }
-  }
-#pragma unroll
-  for (int o = 4; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-  return n;
 }
 
 // Early-out part of calcSolidFraction for one node, decided in FP32 with a
@@ -254,201 +301,303 @@ static __device__ __forceinline__ int classify_node(int hi, int hj, int hk, cons
   return -1;
 }
 
-constexpr int SF_THREADS = 256;
-constexpr int SF_ROUND = 2048;  // box nodes classified per round (queue capacity)
-constexpr int SF_WBUF = 64;     // per-warp buffer of crossing rows
+constexpr int SFC_THREADS = 256;  // classification: one block per image
+constexpr int SFS_THREADS = 128;  // shell counting: persistent warps
+constexpr int SFS_BUF = 352;      // per-warp buffer of crossing rows (>= 32 + 32*10)
 
 static __device__ __forceinline__ float sub_offset(int k) {
   return -0.45f + 0.1f * small_int_to_float(k);  // within 1.7u of the reference's delta_k
 }
 
-// Phase 1 of the map: solid-fraction codes of every node of every image box
-// (independent of image order).  One block per image.  Box nodes are
-// classified per thread; shell nodes go to a shared-memory queue and are then
-// counted one per lane: every lane walks its node's 100 rows of 10 sub-cells
-// in a warp-uniform loop, counting rows wholly inside in registers, and pushes
-// rows that cross the surface into a per-warp buffer that is drained 32 rows
-// at a time, one row per lane (so no lane idles on another's crossing row).
-// Nodes where any sub-cell sum falls inside the FP32 margin are recounted
-// exactly in FP64.
-__global__ void __launch_bounds__(SF_THREADS) sf_kernel(MapParams p) {
+// Phase 1 of the map, one block per image: every node of the image box is
+// classified by the early-out radii of calcSolidFraction; inside / outside
+// nodes get their code here, shell nodes (whose sub-cells must be counted)
+// are queued in shared memory and appended to a global list with one atomic
+// per round of the block.
+constexpr int SFC_ROUND = 2048;
+__global__ void __launch_bounds__(SFC_THREADS) sf_classify_kernel(MapParams p) {
   const Img& im = p.img[blockIdx.x];
   if (!im.valid) return;
   if (p.pair_total[0] > (unsigned long long)p.list_cap ||
       p.pair_total[1] > (unsigned long long)p.sf_cap)
     return;
+  __shared__ int q_li[SFC_ROUND], q_xy[SFC_ROUND], q_z[SFC_ROUND];
+  __shared__ int qn;
+  __shared__ unsigned long long qbase;
   const Geom& g = p.g;
-  const int wx = im.box[0], wy = im.box[1], wz = im.box[2];
-  const int vol = wx * wy * wz;
+  const int wx = im.box[0], wy = im.box[1];
+  const int vol = wx * wy * im.box[2];
   unsigned short* code = p.sfcode + im.sf_off;
-  constexpr int NW = SF_THREADS / 32;
-  __shared__ int queue[SF_ROUND];
-  __shared__ int exact_list[SF_ROUND];
-  __shared__ float buf_s[NW][SF_WBUF];
-  __shared__ int buf_o[NW][SF_WBUF];
-  __shared__ float np_dc[NW][32], np_lo[NW][32], np_hi[NW][32];
-  __shared__ int wcnt[NW][32], wamb[NW][32];
-  __shared__ int qn, nex;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const float u = 5.9604644775390625e-08f;  // 2^-24
   const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
-  for (int base = 0; base < vol; base += SF_ROUND) {
-    if (threadIdx.x == 0) {
-      qn = 0;
-      nex = 0;
-    }
+  for (int r0 = 0; r0 < vol; r0 += SFC_ROUND) {
+    if (threadIdx.x == 0) qn = 0;
     __syncthreads();
-    const int end = min(vol, base + SF_ROUND);
-    for (int li = base + threadIdx.x; li < end; li += SF_THREADS) {
+    const int r1 = min(vol, r0 + SFC_ROUND);
+    for (int li = r0 + threadIdx.x; li < r1; li += SFC_THREADS) {
       const int q1 = (int)fast_div((unsigned)li, fx);
       const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int sx = im.lo[0] + li - q1 * wx;
-      const int sy = im.lo[1] + q1 - q2 * wy;
-      const int sz = im.lo[2] + q2;
+      const int hx = im.lo[0] + li - q1 * wx + g.off[0];
+      const int hy = im.lo[1] + q1 - q2 * wy + g.off[1];
+      const int hz = im.lo[2] + q2 + g.off[2];
       float dxf, dyf, dzf;
-      const int c = classify_node(sx + g.off[0], sy + g.off[1], sz + g.off[2], im, dxf, dyf, dzf);
-      if (c >= 0)
+      const int c = classify_node(hx, hy, hz, im, dxf, dyf, dzf);
+      if (c >= 0) {
         code[li] = (unsigned short)c;
-      else
-        queue[atomicAdd(&qn, 1)] = li;
+      } else {
+        const int k = atomicAdd(&qn, 1);
+        q_li[k] = li;
+        q_xy[k] = hx | (hy << 16);
+        q_z[k] = hz;
+      }
     }
     __syncthreads();
     const int nq = qn;
-    for (int e0 = warp * 32; e0 < nq; e0 += SF_THREADS) {
-      const int e = e0 + lane;
-      const bool valid = e < nq;
-      const int li = valid ? queue[e] : queue[e0];
-      const int q1 = (int)fast_div((unsigned)li, fx);
-      const int q2 = (int)fast_div((unsigned)q1, fy);
-      const float dxf = small_int_to_float(im.lo[0] + li - q1 * wx + g.off[0] - im.xi[0]) - im.xf[0];
-      const float dyf = small_int_to_float(im.lo[1] + q1 - q2 * wy + g.off[1] - im.xi[1]) - im.xf[1];
-      const float dzf = small_int_to_float(im.lo[2] + q2 + g.off[2] - im.xi[2]) - im.xf[2];
-      // axis order: outer a, middle b, inner c along the smallest |d|
+    if (threadIdx.x == 0 && nq) qbase = atomicAdd(&p.pair_total[2], (unsigned long long)nq);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nq; k += SFC_THREADS) {
+      const unsigned long long pos = qbase + k;
+      if (pos < (unsigned long long)p.shell_cap)
+        p.shell[pos] = make_int4((int)blockIdx.x, q_li[k], q_xy[k], q_z[k]);
+      else
+        atomicOr(p.status, STATUS_LIST_OVERFLOW);
+    }
+    __syncthreads();
+  }
+}
+
+// Exact double of a small non-negative integer without the conversion unit.
+static __device__ __forceinline__ double small_int_to_double(int k) {
+  return __hiloint2double(0x43300000, k) - 4503599627370496.0;  // 2^52 + k - 2^52
+}
+
+// One row of sub-cells whose FP32 decision is not certain: the row fixes
+// sub-cell index ia on axis pa and ib on axis pb and runs over the 10
+// indices c of the remaining axis.  Sub-cells whose FP32 c-term lies below
+// the band count as inside, above it as outside, and the ones inside the
+// band are decided with the reference's FP64 expressions
+// (src/LBM_PSM_exchangeParticleData.cpp:144-168).  Kept out of line so that
+// the rare branch calling it is not predicated into every row.
+static __device__ __noinline__ int exact_row_count(const Img& im, int hx, int hy, int hz, int pa,
+                                                   int pb, int ia, int ib, float dc, float tlo,
+                                                   float thi) {
+  const double sliceWidth = 1.0 / ((double)10);
+  const double rSq = im.r * im.r;
+  const double D[3] = {small_int_to_double(hx) - im.xl[0], small_int_to_double(hy) - im.xl[1],
+                       small_int_to_double(hz) - im.xl[2]};
+  int n = 0;
+#pragma unroll
+  for (int c = 0; c < 10; ++c) {
+    const float t = dc + (float)(-0.5 + ((double)c + 0.5) * 0.1);
+    const float sc = t * t;
+    if (sc < tlo) {
+      ++n;
+    } else if (sc <= thi) {
+      const int i0 = pa == 0 ? ia : (pb == 0 ? ib : c);
+      const int i1 = pa == 1 ? ia : (pb == 1 ? ib : c);
+      const int i2 = pa == 2 ? ia : (pb == 2 ? ib : c);
+      const double t0 = D[0] + (-0.5 + (small_int_to_double(i0) + 0.5) * sliceWidth);
+      const double t1 = D[1] + (-0.5 + (small_int_to_double(i1) + 0.5) * sliceWidth);
+      const double t2 = D[2] + (-0.5 + (small_int_to_double(i2) + 0.5) * sliceWidth);
+      const double ax = t0 * t0, ay = t1 * t1, az = t2 * t2;
+      if (ax + ay + az < rSq) ++n;
+    }
+  }
+  return n;
+}
+
+// The same for a whole 2-D node (10 x 10 sub-cells).
+static __device__ __noinline__ int exact_count_2d(const Img& im, int hx, int hy) {
+  const double sliceWidth = 1.0 / ((double)10);
+  const double rSq = im.r * im.r;
+  const double D0 = (double)hx - im.xl[0], D1 = (double)hy - im.xl[1];
+  int n = 0;
+  for (int a = 0; a < 10; ++a) {
+    const double ta = D0 + (-0.5 + ((double)a + 0.5) * sliceWidth);
+    const double ax = ta * ta;
+    for (int b = 0; b < 10; ++b) {
+      const double tb = D1 + (-0.5 + ((double)b + 0.5) * sliceWidth);
+      if (ax + tb * tb < rSq) ++n;
+    }
+  }
+  return n;
+}
+
+// Phase 2: sub-cell counts of the shell nodes, one node per lane, the list
+// walked by a persistent grid in warp-sized chunks.
+//
+// 3-D: with the axes ordered so that the inner axis c has the smallest
+// |offset| (its rows run most nearly along the sphere surface, so fewest of
+// them cross it), each lane walks its node's 100 rows (a, b).  A row whose
+// 10 sub-cell sums are all below r^2 - M counts 10, one whose sums are all
+// above r^2 + M counts 0 (M bounds the FP32 error, 16x the worst case);
+// a row in between crosses the surface and is pushed into a per-warp buffer
+// that is drained 32 rows at a time, one row per lane: the count is the rank
+// of r^2 - M - s_ab among the node's 10 sorted c-terms, and a c-term within
+// the margin band makes the row ambiguous, in which case that row alone is
+// recounted exactly in FP64.
+// 2-D: 100 sub-cells per node, counted in FP32 with the same margin; a node
+// with any ambiguous sub-cell is recounted exactly.
+__global__ void __launch_bounds__(SFS_THREADS) sf_shell_kernel(MapParams p) {
+  constexpr int NW = SFS_THREADS / 32;
+  __shared__ float s_sorted[NW][32][17];  // 10 sorted c-terms + padding (odd stride)
+  __shared__ float s_lo[NW][32];
+  __shared__ float s_hi[NW][32];
+  __shared__ int s_cnt[NW][32];
+  __shared__ int s_ent[NW][32];   // shell-list entry of each lane's node
+  __shared__ int s_perm[NW][32];  // its axis order: pa | pb << 2
+  __shared__ float s_dc[NW][32];  // its inner-axis offset
+  __shared__ float buf_s[NW][SFS_BUF];
+  __shared__ int buf_o[NW][SFS_BUF];
+  const unsigned long long tot = p.pair_total[2];
+  const int total = (int)min(tot, (unsigned long long)p.shell_cap);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * NW + warp, nw = gridDim.x * NW;
+  const float u = 5.9604644775390625e-08f;  // 2^-24
+  const Geom& g = p.g;
+#pragma unroll
+  for (int k = 10; k < 16; ++k) s_sorted[warp][lane][k] = 3.0e38f;
+  for (int base = gw * 32; base < total; base += nw * 32) {
+    const int e = base + lane;
+    const bool valid = e < total;
+    const int4 ent = p.shell[valid ? e : base];
+    const Img& im = p.img[ent.x];
+    const int hx = ent.z & 0xFFFF, hy = ent.z >> 16, hz = ent.w;
+    const float dxf = small_int_to_float(hx - im.xi[0]) - im.xf[0];
+    const float dyf = small_int_to_float(hy - im.xi[1]) - im.xf[1];
+    const float dzf = small_int_to_float(hz - im.xi[2]) - im.xf[2];
+    const float rSqf = im.rSqf;
+    int n = 0;
+    if (g.dim == 2) {
+      const float Ea = fabsf(dxf) + 2.0f, Eb = fabsf(dyf) + 2.0f;
+      const float M = 16.0f * u * (Ea * Ea + Eb * Eb + rSqf);
+      const float lo = rSqf - M, hi = rSqf + M;
+      int amb = 0;
+      for (int a = 0; a < 10; ++a) {
+        const float ta = dxf + sub_offset(a);
+        const float sa = ta * ta;
+#pragma unroll
+        for (int b = 0; b < 10; ++b) {
+          const float tb = dyf + (float)(-0.5 + ((double)b + 0.5) * 0.1);
+          const float t = sa + tb * tb;
+          n += (t < lo);
+          amb += (t >= lo) & (t <= hi);
+        }
+      }
+      if (valid && amb) n = exact_count_2d(im, hx, hy);
+    } else {
+      // axis order: outer a, middle b, inner c along the smallest |offset|
       float da = dxf, db = dyf, dc = dzf;
-      if (g.dim == 3) {
+      int pa = 0, pb = 1;
+      {
         const float ax = fabsf(dxf), ay = fabsf(dyf), az = fabsf(dzf);
         if (ax <= ay && ax <= az) {
-          da = dyf; db = dzf; dc = dxf;
+          da = dyf; db = dzf; dc = dxf; pa = 1; pb = 2;
         } else if (ay <= ax && ay <= az) {
-          da = dxf; db = dzf; dc = dyf;
+          da = dxf; db = dzf; dc = dyf; pa = 0; pb = 2;
         }
       }
       const float Ea = fabsf(da) + 2.0f, Eb = fabsf(db) + 2.0f, Ec = fabsf(dc) + 2.0f;
-      const float Emax = g.dim == 3 ? Ea * Ea + Eb * Eb + Ec * Ec : Ea * Ea + Eb * Eb;
-      const float M = 16.0f * u * (Emax + im.rSqf);
-      const float lo = im.rSqf - M, hi = im.rSqf + M;
-      int n = 0, amb = 0;
-      if (g.dim == 2) {
-        for (int a = 0; a < 10; ++a) {
-          const float ta = da + sub_offset(a);
-          const float sa = ta * ta;
+      const float M = 16.0f * u * (Ea * Ea + Eb * Eb + Ec * Ec + rSqf);
+      const float lo = rSqf - M, hi = rSqf + M;
+      // the 10 c-terms, sorted (odd-even transposition)
+      float sc[10];
 #pragma unroll
-          for (int b = 0; b < 10; ++b) {
-            const float tb = db + (float)(-0.5 + ((double)b + 0.5) * 0.1);
-            const float t = sa + tb * tb;
-            n += (t < lo);
-            amb += (t >= lo) & (t <= hi);
-          }
-        }
-      } else {
-        float cmin = 3.4e38f, cmax = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 10; ++k) {
-          const float t = dc + (float)(-0.5 + ((double)k + 0.5) * 0.1);
-          cmin = fminf(cmin, t * t);
-          cmax = fmaxf(cmax, t * t);
-        }
-        np_dc[warp][lane] = dc;
-        np_lo[warp][lane] = lo;
-        np_hi[warp][lane] = hi;
-        wcnt[warp][lane] = 0;
-        wamb[warp][lane] = 0;
-        __syncwarp();
-        int wcount = 0;
-        for (int a = 0; a < 10; ++a) {
-          const float ta = da + sub_offset(a);
-          const float sa = ta * ta;
-          for (int b = 0; b < 10; ++b) {
-            const float tb = db + sub_offset(b);
-            const float sv = sa + tb * tb;
-            const bool inside = sv + cmax < lo;
-            const bool cross = valid && !inside && !(sv + cmin > hi);
-            n += inside ? 10 : 0;
-            const unsigned m = __ballot_sync(0xffffffffu, cross);
-            if (cross) {
-              const int pos = wcount + __popc(m & ((1u << lane) - 1u));
-              buf_s[warp][pos] = sv;
-              buf_o[warp][pos] = lane;
-            }
-            wcount += __popc(m);
-            if (wcount >= 32) {
-              __syncwarp();
-              const int k = wcount - 32 + lane;
-              const float sk = buf_s[warp][k];
-              const int ow = buf_o[warp][k];
-              const float dco = np_dc[warp][ow], loo = np_lo[warp][ow], hio = np_hi[warp][ow];
-              int nn = 0, na = 0;
-#pragma unroll
-              for (int cc = 0; cc < 10; ++cc) {
-                const float tc = dco + (float)(-0.5 + ((double)cc + 0.5) * 0.1);
-                const float t = sk + tc * tc;
-                nn += (t < loo);
-                na += (t >= loo) & (t <= hio);
-              }
-              if (nn) atomicAdd(&wcnt[warp][ow], nn);
-              if (na) atomicAdd(&wamb[warp][ow], na);
-              wcount -= 32;
-              __syncwarp();
-            }
-          }
-        }
-        __syncwarp();
-        if (lane < wcount) {
-          const float sk = buf_s[warp][lane];
-          const int ow = buf_o[warp][lane];
-          const float dco = np_dc[warp][ow], loo = np_lo[warp][ow], hio = np_hi[warp][ow];
-          int nn = 0, na = 0;
-#pragma unroll
-          for (int cc = 0; cc < 10; ++cc) {
-            const float tc = dco + (float)(-0.5 + ((double)cc + 0.5) * 0.1);
-            const float t = sk + tc * tc;
-            nn += (t < loo);
-            na += (t >= loo) & (t <= hio);
-          }
-          if (nn) atomicAdd(&wcnt[warp][ow], nn);
-          if (na) atomicAdd(&wamb[warp][ow], na);
-        }
-        __syncwarp();
-        n += wcnt[warp][lane];
-        amb += wamb[warp][lane];
-        __syncwarp();
+      for (int c = 0; c < 10; ++c) {
+        const float t = dc + (float)(-0.5 + ((double)c + 0.5) * 0.1);
+        sc[c] = t * t;
       }
-      if (valid) {
-        if (amb == 0)
-          code[li] = (unsigned short)n;
-        else
-          exact_list[atomicAdd(&nex, 1)] = li;
+#pragma unroll
+      for (int r = 0; r < 10; ++r) {
+#pragma unroll
+        for (int c = r & 1; c + 1 < 10; c += 2) {
+          const float x = fminf(sc[c], sc[c + 1]), y = fmaxf(sc[c], sc[c + 1]);
+          sc[c] = x;
+          sc[c + 1] = y;
+        }
       }
+#pragma unroll
+      for (int c = 0; c < 10; ++c) s_sorted[warp][lane][c] = sc[c];
+      s_lo[warp][lane] = lo;
+      s_hi[warp][lane] = hi;
+      s_cnt[warp][lane] = 0;
+      const float lo_in = lo - sc[9];   // row wholly inside: s_ab + max c-term < lo
+      const float hi_out = hi - sc[0];  // row wholly outside: s_ab + min c-term > hi
+      float sb[10];
+#pragma unroll
+      for (int b = 0; b < 10; ++b) {
+        const float t = db + sub_offset(b);
+        sb[b] = t * t;
+      }
+      s_ent[warp][lane] = valid ? e : base;
+      s_perm[warp][lane] = pa | (pb << 2);
+      s_dc[warp][lane] = dc;
+      __syncwarp();
+      // count of one buffered crossing row, added to its owner lane
+      auto drain_row = [&](int k) {
+        const float sv = buf_s[warp][k];
+        const int o = buf_o[warp][k];
+        const int ow = o & 31;
+        const float tlo = s_lo[warp][ow] - sv, thi = s_hi[warp][ow] - sv;
+        const float* srt = s_sorted[warp][ow];
+        int r = 0;  // number of c-terms below tlo (entries 10..15 are +huge)
+        if (srt[r + 7] < tlo) r += 8;
+        if (srt[r + 3] < tlo) r += 4;
+        if (srt[r + 1] < tlo) r += 2;
+        if (srt[r] < tlo) r += 1;
+        int rc = r;
+        if (srt[r] <= thi) {  // a c-term inside the margin band: decide it exactly
+          const int4 oe = p.shell[s_ent[warp][ow]];
+          const int pp = s_perm[warp][ow];
+          rc = exact_row_count(p.img[oe.x], oe.z & 0xFFFF, oe.z >> 16, oe.w, pp & 3, pp >> 2,
+                               (o >> 5) & 15, (o >> 9) & 15, s_dc[warp][ow], tlo, thi);
+        }
+        if (rc) atomicAdd(&s_cnt[warp][ow], rc);
+      };
+      int wtotal = 0;  // rows in the warp buffer (warp-uniform)
+      for (int a = 0; a < 10; ++a) {
+        const float ta = da + sub_offset(a);
+        const float sa = ta * ta;
+        unsigned cm = 0;
+#pragma unroll
+        for (int b = 0; b < 10; ++b) {
+          const float sv = sa + sb[b];
+          const bool inside = sv < lo_in;
+          n += inside ? 10 : 0;
+          cm |= (!inside && sv <= hi_out) ? (1u << b) : 0u;
+        }
+        if (!valid) cm = 0;
+        // append the crossing rows to the warp buffer
+        const int cnt = __popc(cm);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        int pos = wtotal + incl - cnt;
+        while (cm) {
+          const int b = __ffs(cm) - 1;
+          cm &= cm - 1u;
+          const float tb = db + sub_offset(b);
+          buf_s[warp][pos] = sa + tb * tb;
+          buf_o[warp][pos] = lane | (a << 5) | (b << 9);
+          ++pos;
+        }
+        wtotal += __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        // drain 32 rows at a time, one per lane
+        while (wtotal >= 32) {
+          drain_row(wtotal - 32 + lane);
+          wtotal -= 32;
+          __syncwarp();
+        }
+      }
+      if (lane < wtotal) drain_row(lane);
+      __syncwarp();
+      n += s_cnt[warp][lane];
+      __syncwarp();
     }
-    __syncthreads();
-    // exact FP64 recount of the ambiguous nodes, four per warp
-    const int ne = nex;
-    const int grp = lane >> 3, sub = lane & 7;
-    for (int e0 = warp * 4; e0 < ne; e0 += NW * 4) {
-      const int e = e0 + grp;
-      const bool valid = e < ne;
-      const int li = valid ? exact_list[e] : 0;
-      const int q1 = (int)fast_div((unsigned)li, fx);
-      const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int hi = im.lo[0] + li - q1 * wx + g.off[0];
-      const int hj = im.lo[1] + q1 - q2 * wy + g.off[1];
-      const int hk = im.lo[2] + q2 + g.off[2];
-      const int nc = subcell_count_exact_group8(valid, g.dim, (double)hi - im.xl[0],
-                                                (double)hj - im.xl[1], (double)hk - im.xl[2],
-                                                im.r, sub);
-      if (valid && sub == 0) code[li] = (unsigned short)nc;
-    }
-    __syncthreads();
+    if (valid) p.sfcode[im.sf_off + ent.y] = (unsigned short)n;
   }
 }
 
@@ -467,6 +616,12 @@ __global__ void __launch_bounds__(SF_THREADS) sf_kernel(MapParams p) {
 // sf_old > 1e-5 means the tag matched), so only the sf bit decides.  sf > 1e-5
 // exactly when the code is non-zero.  The table is written back only where it
 // changed.
+// Bit equality of two doubles as two 32-bit compares (64-bit integer
+// compares take the slow path on this GPU).
+static __device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double2loint(a) == __double2loint(b) && __double2hiint(a) == __double2hiint(b);
+}
+
 __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
   const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
   const int cnt = p.cell_count[c];
@@ -553,13 +708,10 @@ __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
       u2 = im.uT[2];
     }
     // re-setting a slot to the values it already holds changes nothing
-    bool same = !slot_dirty[slot] && id[slot] == tag &&
-                __double_as_longlong(eps[slot]) == __double_as_longlong(sf);
+    bool same = !slot_dirty[slot] && id[slot] == tag && same_bits(eps[slot], sf);
     if (same) {
       const double* cur = p.tab.us + 6 * n + 3 * slot;
-      same = __double_as_longlong(cur[0]) == __double_as_longlong(u0) &&
-             __double_as_longlong(cur[1]) == __double_as_longlong(u1) &&
-             __double_as_longlong(cur[2]) == __double_as_longlong(u2);
+      same = same_bits(cur[0], u0) && same_bits(cur[1], u1) && same_bits(cur[2], u2);
     }
     if (!same) {
       if (id[slot] != tag) ids_dirty = true;
@@ -589,11 +741,13 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   if (p.n <= 0) return cudaSuccess;
   const int ncells = p.C[0] * p.C[1] * p.C[2];
   const int tb = 128;
+  const unsigned wblocks = (unsigned)(((long long)p.n * 32 + tb - 1) / tb);
   img_prep_kernel<<<(p.n + tb - 1) / tb, tb, 0, st>>>(p);
-  cell_scan_kernel<<<1, 1024, 0, st>>>(p.cell_count, p.cell_off, ncells);
-  img_fill_kernel<<<(p.n + tb - 1) / tb, tb, 0, st>>>(p);
+  cell_scan_kernel<<<1, SCAN_THREADS, 0, st>>>(p.cell_count, p.cell_off, ncells);
+  img_fill_kernel<<<wblocks, tb, 0, st>>>(p);
   cell_sort_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(p, ncells);
-  sf_kernel<<<p.n, SF_THREADS, 0, st>>>(p);
+  sf_classify_kernel<<<p.n, SFC_THREADS, 0, st>>>(p);
+  sf_shell_kernel<<<p.sm_count * 8, SFS_THREADS, 0, st>>>(p);
   dim3 block(p.cb[0], p.cb[1], p.cb[2]);
   dim3 cells((unsigned)p.C[0], (unsigned)p.C[1], (unsigned)p.C[2]);
   node_apply_kernel<<<cells, block, 0, st>>>(p);
@@ -602,42 +756,6 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
 
 // ------------------------------------------------------------------ reduce
 constexpr int RED_THREADS = 256;
-
-// Box of one image clamped to interior nodes (src/LBM_PSM_exchangeParticleData.cpp:188-195).
-struct RedBox {
-  double xl[3];
-  int lo[3], hi[3];
-};
-
-static __device__ __forceinline__ RedBox reduce_box(const ReduceParams& p, int ip) {
-  const Geom& g = p.g;
-  RedBox b;
-  const double r = p.radius[ip] / p.dx;
-  for (int d = 0; d < 3; ++d) {
-    b.xl[d] = local_centre(p.x[3 * ip + d], p.origin[d], p.dx);
-    int a = (int)(b.xl[d] - r) - 2;
-    int c = (int)(b.xl[d] + r) + 2;
-    if (d < 2 || g.dim == 3) {
-      a = clampi(a, 1, g.L[d] - 1);
-      c = clampi(c, 1, g.L[d] - 1);
-      if (d == 2) {
-        if (a < 0) a = 0;
-        if (c < 1) c = 1;
-      }
-    } else {
-      // fmax(fmin(fmax(z, 1), nz - 1), slot) with nz = 1 in 2-D
-      a = a < 1 ? 1 : a;
-      a = a > g.L[2] - 1 ? g.L[2] - 1 : a;
-      a = a < 0 ? 0 : a;
-      c = c < 1 ? 1 : c;
-      c = c > g.L[2] - 1 ? g.L[2] - 1 : c;
-      c = c < 1 ? 1 : c;
-    }
-    b.lo[d] = a;
-    b.hi[d] = c;
-  }
-  return b;
-}
 
 static __device__ __forceinline__ void block_reduce_store(double (&acc)[12], const ReduceParams& p,
                                                           int ip) {
@@ -668,8 +786,8 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
   const int ip = blockIdx.x;
   const Geom& g = p.g;
   const int tag = p.tag[ip];
-  const RedBox bx = reduce_box(p, ip);
-  const int wx = bx.hi[0] - bx.lo[0], wy = bx.hi[1] - bx.lo[1], wz = bx.hi[2] - bx.lo[2];
+  const Img& bx = p.img[ip];  // box and centre from the map's image record
+  const int wx = bx.rhi[0] - bx.rlo[0], wy = bx.rhi[1] - bx.rlo[1], wz = bx.rhi[2] - bx.rlo[2];
   double acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k] = 0.0;
@@ -677,13 +795,14 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
     const long long total = (long long)wx * wy * wz;
     const double ff = p.forceFactor, tf = p.torqueFactor;
     const double* nodeF = static_cast<const double*>(p.tab.nodeF);
-    const FastDiv fz = make_fastdiv((unsigned)wz), fy = make_fastdiv((unsigned)wy);
+    // x fastest: consecutive threads read consecutive nodes
+    const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
     for (long long t = threadIdx.x; t < total; t += RED_THREADS) {
-      const int q1 = (int)fast_div((unsigned)t, fz);
+      const int q1 = (int)fast_div((unsigned)t, fx);
       const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int k = bx.lo[2] + (int)t - q1 * wz;
-      const int j = bx.lo[1] + q1 - q2 * wy;
-      const int i = bx.lo[0] + q2;
+      const int i = bx.rlo[0] + (int)t - q1 * wx;
+      const int j = bx.rlo[1] + q1 - q2 * wy;
+      const int k = bx.rlo[2] + q2;
       const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
       const int2 id = p.tab.ids[n];
       int slot;
@@ -733,28 +852,24 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
   const int ip = blockIdx.x;
   const Geom& g = p.g;
   const int tag = p.tag[ip];
-  const RedBox bx = reduce_box(p, ip);
-  const int wx = bx.hi[0] - bx.lo[0], wy = bx.hi[1] - bx.lo[1], wz = bx.hi[2] - bx.lo[2];
+  const Img& bx = p.img[ip];  // box and centre from the map's image record
+  const int wx = bx.rhi[0] - bx.rlo[0], wy = bx.rhi[1] - bx.rlo[1], wz = bx.rhi[2] - bx.rlo[2];
   float hi[12], lo[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) hi[k] = lo[k] = 0.0f;
   if (wx > 0 && wy > 0 && wz > 0) {
-    int xi[3];
-    float xf[3];
-    for (int d = 0; d < 3; ++d) {
-      const double fl = fabs(bx.xl[d]) < 1.0e9 ? floor(bx.xl[d]) : 0.0;
-      xi[d] = (int)fl;
-      xf[d] = (float)(bx.xl[d] - fl);
-    }
+    const int xi[3] = {bx.xi[0], bx.xi[1], bx.xi[2]};  // xl = xi + xf exactly
+    const float xf[3] = {bx.xf[0], bx.xf[1], bx.xf[2]};
     const int total = wx * wy * wz;
     const float* nodeF = static_cast<const float*>(p.tab.nodeF);
-    const FastDiv fz = make_fastdiv((unsigned)wz), fy = make_fastdiv((unsigned)wy);
+    // x fastest: consecutive threads read consecutive nodes
+    const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
     for (int t = threadIdx.x; t < total; t += RED_THREADS) {
-      const int q1 = (int)fast_div((unsigned)t, fz);
+      const int q1 = (int)fast_div((unsigned)t, fx);
       const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int k = bx.lo[2] + t - q1 * wz;
-      const int j = bx.lo[1] + q1 - q2 * wy;
-      const int i = bx.lo[0] + q2;
+      const int i = bx.rlo[0] + t - q1 * wx;
+      const int j = bx.rlo[1] + q1 - q2 * wy;
+      const int k = bx.rlo[2] + q2;
       const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
       const int2 id = p.tab.ids[n];
       int slot;
@@ -803,15 +918,25 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
       lo[q] = lo[q] + l2 + e;
     }
   }
-  __shared__ double part[RED_THREADS / 32][12];
+  // warps in index order, still in double-float; one FP64 sum per term
+  __shared__ float part_hi[RED_THREADS / 32][12], part_lo[RED_THREADS / 32][12];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
-    for (int q = 0; q < 12; ++q) part[warp][q] = (double)hi[q] + (double)lo[q];
+    for (int q = 0; q < 12; ++q) {
+      part_hi[warp][q] = hi[q];
+      part_lo[warp][q] = lo[q];
+    }
   __syncthreads();
   if (threadIdx.x < 12) {
     const int q = threadIdx.x;
-    double sum = 0.0;
-    for (int w = 0; w < RED_THREADS / 32; ++w) sum += part[w][q];
+    float sh = 0.0f, sl = 0.0f;
+    for (int w = 0; w < RED_THREADS / 32; ++w) {
+      float sv, e;
+      two_sum(sh, part_hi[w][q], sv, e);
+      sh = sv;
+      sl = sl + part_lo[w][q] + e;
+    }
+    const double sum = (double)sh + (double)sl;
     if (q < 3)
       p.fh[3 * ip + q] = sum * p.forceFactor;
     else if (q < 6)
