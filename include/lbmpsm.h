@@ -173,7 +173,9 @@ int lbmpsm_get_populations(lbmpsm_handle* h, double* f);
 int lbmpsm_set_populations(lbmpsm_handle* h, const double* f);
 /* Particle table per node in the reference layout: ids[2N], eps[2N],
  * us[6N] (LBMPSMLattice::getParticleDataOnLatticeNode,
- * src/LBM_PSM_lattice.cpp:255).  Halo nodes of periodic axes read as empty. */
+ * src/LBM_PSM_lattice.cpp:255).  Halo nodes of periodic axes read as empty.
+ * FP64 storage keeps eps and us in FP64 (the reference's values bit for bit);
+ * FP32 / FP16 storage keeps only their FP32 roundings, returned widened. */
 int lbmpsm_get_particle_table(lbmpsm_handle* h, int* ids, double* eps, double* us);
 
 /* Global FP64 check (no reference counterpart): total mass and momentum of

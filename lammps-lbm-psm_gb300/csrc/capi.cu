@@ -63,6 +63,7 @@ struct lbmpsm_handle {
   int* d_status = nullptr;
   double* d_check = nullptr;
   double* d_sf_value = nullptr;  // n/10^d for n = 0..1000
+  float* d_sf_value32 = nullptr;  // its FP32 roundings
   void* h_stage = nullptr;  // pinned: inputs then outputs
   size_t h_stage_bytes = 0;
   int last_n = 0;
@@ -388,6 +389,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     m.sfcode = h->d_sfcode;
     m.sf_cap = h->sf_cap;
     m.sf_value = h->d_sf_value;
+    m.sf_value32 = h->d_sf_value32;
     m.shell = h->d_shell;
     m.shell_cap = h->sf_cap;
     m.sm_count = h->sm_count;
@@ -582,18 +584,23 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
   if (dmalloc(h, &h->f, es * (size_t)g.Np * g.Q) != cudaSuccess ||
       dmalloc(h, &h->tab.flag, N) != cudaSuccess ||
       dmalloc(h, &h->tab.ids, sizeof(int2) * N) != cudaSuccess ||
-      dmalloc(h, &h->tab.eps, sizeof(double2) * N) != cudaSuccess ||
-      dmalloc(h, &h->tab.us, sizeof(double) * 6 * N) != cudaSuccess ||
       dmalloc(h, &h->tab.nodeF, (o.storage == 0 ? 8 : 4) * 6 * N) != cudaSuccess)
     return bail(LBMPSM_ERR_NOMEM);
-  if (o.storage != 0 && dmalloc(h, &h->tab.rec32, sizeof(float4) * 2 * N) != cudaSuccess)
+  // FP64 storage keeps the table in FP64; the other storages only the FP32 records
+  if (o.storage == LBMPSM_STORAGE_FP64 &&
+      (dmalloc(h, &h->tab.eps, sizeof(double2) * N) != cudaSuccess ||
+       dmalloc(h, &h->tab.us, sizeof(double) * 6 * N) != cudaSuccess))
+    return bail(LBMPSM_ERR_NOMEM);
+  if (o.storage != LBMPSM_STORAGE_FP64 &&
+      dmalloc(h, &h->tab.rec32, sizeof(float4) * 2 * N) != cudaSuccess)
     return bail(LBMPSM_ERR_NOMEM);
   const int ncells = h->C[0] * h->C[1] * h->C[2];
   if (dmalloc(h, &h->d_cells, sizeof(int) * 3 * (size_t)ncells) != cudaSuccess ||
       dmalloc(h, &h->d_pair_total, 4 * sizeof(unsigned long long)) != cudaSuccess ||
       dmalloc(h, &h->d_status, sizeof(int)) != cudaSuccess ||
       dmalloc(h, &h->d_check, sizeof(double) * (4 + 4 * 1024)) != cudaSuccess ||
-      dmalloc(h, &h->d_sf_value, sizeof(double) * 1001) != cudaSuccess)
+      dmalloc(h, &h->d_sf_value, sizeof(double) * 1001) != cudaSuccess ||
+      dmalloc(h, &h->d_sf_value32, sizeof(float) * 1001) != cudaSuccess)
     return bail(LBMPSM_ERR_NOMEM);
   {
     // calcSolidFraction's return value fraction*n (src/LBM_PSM_exchangeParticleData.cpp:165,213)
@@ -602,13 +609,16 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
     double fraction = 1.0 / ((double)(slices * slices));
     if (g.dim == 3) fraction = 1.0 / ((double)(slices * slices * slices));
     for (int k = 0; k <= 1000; ++k) tbl[k] = fraction * ((double)k);
-    if (cudaMemcpy(h->d_sf_value, tbl, sizeof(tbl), cudaMemcpyHostToDevice) != cudaSuccess)
+    float tbl32[1001];
+    for (int k = 0; k <= 1000; ++k) tbl32[k] = (float)tbl[k];
+    if (cudaMemcpy(h->d_sf_value, tbl, sizeof(tbl), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->d_sf_value32, tbl32, sizeof(tbl32), cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(LBMPSM_ERR_CUDA);
   }
   cudaMemsetAsync(h->tab.flag, 0, N, h->stream);
   cudaMemsetAsync(h->tab.ids, 0, sizeof(int2) * N, h->stream);
-  cudaMemsetAsync(h->tab.eps, 0, sizeof(double2) * N, h->stream);
-  cudaMemsetAsync(h->tab.us, 0, sizeof(double) * 6 * N, h->stream);
+  if (h->tab.eps) cudaMemsetAsync(h->tab.eps, 0, sizeof(double2) * N, h->stream);
+  if (h->tab.us) cudaMemsetAsync(h->tab.us, 0, sizeof(double) * 6 * N, h->stream);
   cudaMemsetAsync(h->tab.nodeF, 0, (o.storage == 0 ? 8 : 4) * 6 * N, h->stream);
   if (h->tab.rec32) cudaMemsetAsync(h->tab.rec32, 0, sizeof(float4) * 2 * N, h->stream);
   cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream);
@@ -656,6 +666,7 @@ void lbmpsm_destroy(lbmpsm_handle* h) {
   dfree(h->d_status);
   dfree(h->d_check);
   dfree(h->d_sf_value);
+  dfree(h->d_sf_value32);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }

@@ -146,8 +146,8 @@ __device__ __forceinline__ bool nbr_ok(const Nbr& nb, int cx, int cy, int cz) {
 struct Table {
   uint8_t* flag;   // N
   int2* ids;       // N
-  double2* eps;    // N
-  double* us;      // 6N  (slot-major: us[6n + 3*slot + c])
+  double2* eps;    // N (FP64 storage only; null otherwise)
+  double* us;      // 6N  (slot-major: us[6n + 3*slot + c]; FP64 storage only)
   float4* rec32;   // 2N  (eps, usx, usy, usz) per slot, FP32 mirror
   void* nodeF;     // 6N  FP64 (FP64 storage) or FP32 (other storages)
 };
@@ -246,6 +246,7 @@ struct Img {
   long long sf_off;   // offset of this image's box in the solid-fraction code scratch
   int box[3];         // box extents (hi - lo)
   int rlo[3], rhi[3]; // force-reduction box, reference frame, clamped to interior nodes
+  float uTf[3], omf[3];  // FP32 roundings of uT and om (FP32 / FP16 storage)
 };
 
 // Solid-fraction codes of one (image, node) pair: 0..1000 = number of
@@ -276,6 +277,7 @@ struct MapParams {
   unsigned short* sfcode;          // codes of all (image, box node) pairs
   long long sf_cap;
   const double* sf_value;          // sf_value[n] = n/10^d (n = 0..1000), FP64
+  const float* sf_value32;         // its FP32 roundings
   int4* shell;                     // shell nodes: image, box index, x | y << 16, z
   long long shell_cap;
   int sm_count;                    // multiprocessors (persistent grids)

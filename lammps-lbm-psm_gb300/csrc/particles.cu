@@ -108,6 +108,8 @@ __global__ void img_prep_kernel(MapParams p) {
       if (slo >= shi) valid = false;
       im.uT[d] = p.v[3 * i + d] / p.Uc * p.u_lb;
       im.om[d] = p.omega[3 * i + d] * p.tc * p.dt_d;
+      im.uTf[d] = (float)im.uT[d];
+      im.omf[d] = (float)im.om[d];
     }
     im.valid = valid;
     const double rP = r + p.sqrt2half;
@@ -622,6 +624,7 @@ static __device__ __forceinline__ bool same_bits(double a, double b) {
   return __double2loint(a) == __double2loint(b) && __double2hiint(a) == __double2hiint(b);
 }
 
+// FP64 storage: the table in FP64 (ids, eps, us) with the FP32 mirror.
 __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
   const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
   const int cnt = p.cell_count[c];
@@ -737,6 +740,109 @@ __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
   }
 }
 
+
+// FP32 / FP16 storage: the table is ids + the FP32 records the collide
+// kernel reads (eps, u_s per slot); the same update rules, no FP64.  The
+// records hold the FP32 roundings of the reference's values (for spinning
+// images the node velocity is formed in FP32).
+__global__ void __launch_bounds__(512) node_apply32_kernel(MapParams p) {
+  const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
+  const int cnt = p.cell_count[c];
+  if (cnt == 0) return;
+  if (p.pair_total[0] > (unsigned long long)p.list_cap ||
+      p.pair_total[1] > (unsigned long long)p.sf_cap)
+    return;
+  const Geom& g = p.g;
+  const int sx = blockIdx.x * p.cb[0] + threadIdx.x;
+  const int sy = blockIdx.y * p.cb[1] + threadIdx.y;
+  const int sz = blockIdx.z * p.cb[2] + threadIdx.z;
+  if (sx >= g.S[0] || sy >= g.S[1] || sz >= g.S[2]) return;
+  const long long n = node_index(g, sx, sy, sz);
+  const int hi = sx + g.off[0], hj = sy + g.off[1], hk = sz + g.off[2];
+  const int* lst = p.list + p.cell_off[c];
+  int id[2] = {0, 0};
+  float4 rec[2];
+  bool have_ids = false, ids_dirty = false;
+  bool have_rec[2] = {false, false}, slot_dirty[2] = {false, false};
+  for (int t = 0; t < cnt; ++t) {
+    const Img& im = p.img[lst[t]];
+    if (sx < im.lo[0] || sx >= im.hi[0] || sy < im.lo[1] || sy >= im.hi[1] || sz < im.lo[2] ||
+        sz >= im.hi[2])
+      continue;
+    const int li = ((sz - im.lo[2]) * im.box[1] + (sy - im.lo[1])) * im.box[0] + (sx - im.lo[0]);
+    const unsigned short cd = p.sfcode[im.sf_off + li];
+    const int tag = im.tag;
+    if (!have_ids) {
+      const int2 v = p.tab.ids[n];
+      id[0] = v.x;
+      id[1] = v.y;
+      have_ids = true;
+    }
+    const int match = tag == id[0] ? 0 : (tag == id[1] ? 1 : -1);
+    if (cd == 0) {  // setToZero (src/LBM_PSM_lattice.cpp:302-324)
+      if (match >= 0) {
+        id[match] = 0;
+        rec[match] = make_float4(0.f, 0.f, 0.f, 0.f);
+        have_rec[match] = true;
+        ids_dirty = true;
+        slot_dirty[match] = true;
+      }
+      continue;
+    }
+    // setParticleOnLattice: matching slot, else the first empty one, else drop
+    int slot = -1;
+    if (id[0] == tag)
+      slot = 0;
+    else if (id[1] == tag)
+      slot = 1;
+    else if (id[0] == 0)
+      slot = 0;
+    else if (id[1] == 0)
+      slot = 1;
+    if (slot < 0) continue;
+    float4 nv;
+    nv.x = cd == SF_ONE ? 1.0f : p.sf_value32[cd];
+    // rigid-body velocity of the node (src/LBM_PSM_exchangeParticleData.cpp:83-89)
+    if (im.has_spin) {
+      const float dx = small_int_to_float(hi - im.xi[0]) - im.xf[0];
+      const float dy = small_int_to_float(hj - im.xi[1]) - im.xf[1];
+      const float dz = small_int_to_float(hk - im.xi[2]) - im.xf[2];
+      nv.y = im.uTf[0] + im.omf[1] * dz - im.omf[2] * dy;
+      nv.z = im.uTf[1] + im.omf[2] * dx - im.omf[0] * dz;
+      nv.w = im.uTf[2] + im.omf[0] * dy - im.omf[1] * dx;
+    } else {
+      nv.y = im.uTf[0];
+      nv.z = im.uTf[1];
+      nv.w = im.uTf[2];
+    }
+    // re-setting a slot to the values it already holds changes nothing
+    bool same = false;
+    if (!slot_dirty[slot] && id[slot] == tag) {
+      if (!have_rec[slot]) {
+        rec[slot] = p.tab.rec32[2 * n + slot];
+        have_rec[slot] = true;
+      }
+      same = __float_as_int(rec[slot].x) == __float_as_int(nv.x) &&
+             __float_as_int(rec[slot].y) == __float_as_int(nv.y) &&
+             __float_as_int(rec[slot].z) == __float_as_int(nv.z) &&
+             __float_as_int(rec[slot].w) == __float_as_int(nv.w);
+    }
+    if (!same) {
+      if (id[slot] != tag) ids_dirty = true;
+      id[slot] = tag;
+      rec[slot] = nv;
+      have_rec[slot] = true;
+      slot_dirty[slot] = true;
+    }
+  }
+  if (ids_dirty) {
+    p.tab.ids[n] = make_int2(id[0], id[1]);
+    p.tab.flag[n] = (uint8_t)((id[0] > 0 ? 1 : 0) | (id[1] > 0 ? 2 : 0));
+  }
+  if (slot_dirty[0]) p.tab.rec32[2 * n] = rec[0];
+  if (slot_dirty[1]) p.tab.rec32[2 * n + 1] = rec[1];
+}
+
 cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   if (p.n <= 0) return cudaSuccess;
   const int ncells = p.C[0] * p.C[1] * p.C[2];
@@ -750,7 +856,10 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   sf_shell_kernel<<<p.sm_count * 8, SFS_THREADS, 0, st>>>(p);
   dim3 block(p.cb[0], p.cb[1], p.cb[2]);
   dim3 cells((unsigned)p.C[0], (unsigned)p.C[1], (unsigned)p.C[2]);
-  node_apply_kernel<<<cells, block, 0, st>>>(p);
+  if (p.write32)
+    node_apply32_kernel<<<cells, block, 0, st>>>(p);
+  else
+    node_apply_kernel<<<cells, block, 0, st>>>(p);
   return cudaGetLastError();
 }
 
@@ -972,8 +1081,15 @@ __global__ void table_export_kernel(Geom g, Table t, int* ids, double* eps, doub
   if (ok) {
     const long long n = node_index(g, sx, sy, sz);
     id = t.ids[n];
-    e = t.eps[n];
-    for (int c = 0; c < 6; ++c) u[c] = t.us[6 * n + c];
+    if (t.eps) {
+      e = t.eps[n];
+      for (int c = 0; c < 6; ++c) u[c] = t.us[6 * n + c];
+    } else {  // FP32 / FP16 storage keeps only the FP32 records
+      const float4 r0 = t.rec32[2 * n], r1 = t.rec32[2 * n + 1];
+      e = make_double2(r0.x, r1.x);
+      u[0] = r0.y; u[1] = r0.z; u[2] = r0.w;
+      u[3] = r1.y; u[4] = r1.z; u[5] = r1.w;
+    }
   }
   if (ids) {
     ids[2 * r] = id.x;
@@ -1007,7 +1123,7 @@ __global__ void export_fields_kernel(Geom g, Table t, const double* rho, const d
   const int k = (g.dim == 3 ? 1 : 0) + (int)(id / ((long long)nxi * nyi));
   const int sx = i - g.off[0], sy = j - g.off[1], sz = k - g.off[2];
   const long long n = node_index(g, sx, sy, sz);
-  const double2 e = t.eps[n];
+  const double2 e = t.eps ? t.eps[n] : make_double2(t.rec32[2 * n].x, t.rec32[2 * n + 1].x);
   const double Bv = (e.x + e.y);
   const double sv = (Bv > 1.0 ? 1.0 : Bv) * B0;
   const double rv = (rho ? rho[n] : 1.0) * rho0;
