@@ -247,6 +247,8 @@ struct Img {
   int box[3];         // box extents (hi - lo)
   int rlo[3], rhi[3]; // force-reduction box, reference frame, clamped to interior nodes
   float uTf[3], omf[3];  // FP32 roundings of uT and om (FP32 / FP16 storage)
+  int solo;           // no periodic copy of the particle can have an overlapping box
+  int qlo[3], qhi[3]; // part of the reduction box the reduction visits
 };
 
 // Solid-fraction codes of one (image, node) pair: 0..1000 = number of

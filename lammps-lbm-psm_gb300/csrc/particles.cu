@@ -137,6 +137,28 @@ __global__ void img_prep_kernel(MapParams p) {
     }
     im.has_spin = plain ? 0 : 1;
     reduce_box_of(g, im.xl, r, im.rlo, im.rhi);
+    // When no periodic copy of this particle can have an overlapping box
+    // (box width below the period on every periodic axis), the nodes of the
+    // box that hold its tag after the map all have eps > 0 from this image,
+    // hence lie within the early-out radius rP: the reduction then only
+    // visits the box part around the sphere (and still checks each tag).
+    {
+      bool solo = true;
+      for (int d = 0; d < g.dim; ++d) {
+        const int w = ((int)(im.xl[d] + r) + 2) - ((int)(im.xl[d] - r) - 2);
+        if (g.per[d] && w >= g.S[d]) solo = false;
+      }
+      im.solo = solo ? 1 : 0;
+      for (int d = 0; d < 3; ++d) {
+        im.qlo[d] = im.rlo[d];
+        im.qhi[d] = im.rhi[d];
+        if (solo && (d < 2 || g.dim == 3)) {
+          const int a = (int)floor(im.xl[d] - rP), b = (int)floor(im.xl[d] + rP) + 1;
+          im.qlo[d] = max(im.qlo[d], a);
+          im.qhi[d] = min(im.qhi[d], b);
+        }
+      }
+    }
     for (int d = 0; d < 3; ++d) im.box[d] = valid ? im.hi[d] - im.lo[d] : 0;
     if (valid) {
       vol = (unsigned long long)im.box[0] * im.box[1] * im.box[2];
@@ -866,6 +888,19 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
 // ------------------------------------------------------------------ reduce
 constexpr int RED_THREADS = 256;
 
+// Node (i, j, k) lies beyond the early-out radius rP of the image for
+// certain (FP32 distance with the margin proven for classify_node), so its
+// solid fraction for this image is 0.
+static __device__ __forceinline__ bool beyond_rP(const Img& im, int i, int j, int k) {
+  const float u = 5.9604644775390625e-08f;  // 2^-24
+  const float dx = small_int_to_float(i - im.xi[0]) - im.xf[0];
+  const float dy = small_int_to_float(j - im.xi[1]) - im.xf[1];
+  const float dz = small_int_to_float(k - im.xi[2]) - im.xf[2];
+  const float d32 = dx * dx + dy * dy + dz * dz;
+  const float m = 16.0f * u * (5.0f * d32 + 2.0f * (fabsf(dx) + fabsf(dy) + fabsf(dz)) + 1.0f + im.rP2f);
+  return d32 > im.rP2f + m;
+}
+
 static __device__ __forceinline__ void block_reduce_store(double (&acc)[12], const ReduceParams& p,
                                                           int ip) {
   // fixed-order reduction: butterfly within warps, then warps in index order
@@ -896,7 +931,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
   const Geom& g = p.g;
   const int tag = p.tag[ip];
   const Img& bx = p.img[ip];  // box and centre from the map's image record
-  const int wx = bx.rhi[0] - bx.rlo[0], wy = bx.rhi[1] - bx.rlo[1], wz = bx.rhi[2] - bx.rlo[2];
+  const int wx = bx.qhi[0] - bx.qlo[0], wy = bx.qhi[1] - bx.qlo[1], wz = bx.qhi[2] - bx.qlo[2];
   double acc[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) acc[k] = 0.0;
@@ -909,9 +944,10 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
     for (long long t = threadIdx.x; t < total; t += RED_THREADS) {
       const int q1 = (int)fast_div((unsigned)t, fx);
       const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int i = bx.rlo[0] + (int)t - q1 * wx;
-      const int j = bx.rlo[1] + q1 - q2 * wy;
-      const int k = bx.rlo[2] + q2;
+      const int i = bx.qlo[0] + (int)t - q1 * wx;
+      const int j = bx.qlo[1] + q1 - q2 * wy;
+      const int k = bx.qlo[2] + q2;
+      if (bx.solo && beyond_rP(bx, i, j, k)) continue;
       const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
       const int2 id = p.tab.ids[n];
       int slot;
@@ -962,7 +998,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
   const Geom& g = p.g;
   const int tag = p.tag[ip];
   const Img& bx = p.img[ip];  // box and centre from the map's image record
-  const int wx = bx.rhi[0] - bx.rlo[0], wy = bx.rhi[1] - bx.rlo[1], wz = bx.rhi[2] - bx.rlo[2];
+  const int wx = bx.qhi[0] - bx.qlo[0], wy = bx.qhi[1] - bx.qlo[1], wz = bx.qhi[2] - bx.qlo[2];
   float hi[12], lo[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) hi[k] = lo[k] = 0.0f;
@@ -976,9 +1012,10 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
     for (int t = threadIdx.x; t < total; t += RED_THREADS) {
       const int q1 = (int)fast_div((unsigned)t, fx);
       const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int i = bx.rlo[0] + t - q1 * wx;
-      const int j = bx.rlo[1] + q1 - q2 * wy;
-      const int k = bx.rlo[2] + q2;
+      const int i = bx.qlo[0] + t - q1 * wx;
+      const int j = bx.qlo[1] + q1 - q2 * wy;
+      const int k = bx.qlo[2] + q2;
+      if (bx.solo && beyond_rP(bx, i, j, k)) continue;
       const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
       const int2 id = p.tab.ids[n];
       int slot;
