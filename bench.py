@@ -236,10 +236,11 @@ def run_ours(args, rank=0, world=1):
         lt.apply_bc()
         fts = owner_forces(lt)
         u = lt.export_fields(1.0, 1.0, 1.0, as_double=True)[2]
-        return fts, u
+        return fts, u, lt.check()[0]
 
     # FP32 storage: the headline path
     lat = make(args.storage)
+    mass0 = lat.check()[0]
     lat.step(g.tag, g.x, g.v, g.omega, g.radius)  # images go up once, map + step
     lat.apply_bc()
     with ClockSampler(device) as clk:
@@ -290,14 +291,16 @@ def run_ours(args, rank=0, world=1):
 
         def rel(a, b):
             return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
-        (F32, T32, S32), u32 = acc32
-        (F64, T64, S64), u64 = acc64
+        (F32, T32, S32), u32, m32 = acc32
+        (F64, T64, S64), u64, m64 = acc64
         accuracy = {
             "vs": "FP64 GPU path (bit-identical to the CPU oracle on the parity cases)",
             "step": 2 + W + K,
             "drag": rel(F32, F64), "torque": rel(T32, T64), "stresslet": rel(S32, S64),
             "velocity_l2": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
             "velocity_max": rel(u32, u64),
+            "mass_drift_fp32": float((m32 - mass0) / mass0),
+            "mass_drift_fp64": float((m64 - mass0) / mass0),
             "metric": "max |x32 - x64| / max |x64| over particles (F, T, S) or nodes (u)",
         }
 
