@@ -320,6 +320,93 @@ class FixLbmPsmVTI:
                          rho.astype(T), u.astype(T), self.binary)
 
 
+def restart_file_name(rank: int = 0) -> str:
+    """File name of one rank's restart file (src/fix_LBM_PSM_writeReadRestart.cpp:64-67)."""
+    return f"LBM-PSM-restartFile-processor-{rank}.bin"
+
+
+def write_restart(path: str, f: np.ndarray):
+    """LBMPSMWriteReadRestart::write_restart (src/fix_LBM_PSM_writeReadRestart.cpp:80-89):
+    the number of doubles as a native 32-bit unsigned integer, then the
+    populations of the local array (halo included) in the reference layout."""
+    f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+    if f.size >= 2 ** 32:
+        raise LammpsError("lbm-psm-restart: local array too large for the 32-bit size field")
+    with open(path, "wb") as fh:
+        fh.write(np.array([f.size], dtype=np.uint32).tobytes())
+        fh.write(f.tobytes())
+
+
+def read_restart(path: str) -> np.ndarray:
+    """LBMPSMWriteReadRestart::read_restart (src/fix_LBM_PSM_writeReadRestart.cpp:92-103)."""
+    with open(path, "rb") as fh:
+        head = fh.read(4)
+        if len(head) != 4:
+            raise LammpsError(f"lbm-psm-restart: cannot read {path}")
+        n = int(np.frombuffer(head, dtype=np.uint32)[0])
+        data = fh.read(8 * n)
+    if len(data) != 8 * n:
+        raise LammpsError(f"lbm-psm-restart: {path} holds fewer than {n} values")
+    return np.frombuffer(data, dtype=np.float64).copy()
+
+
+class FixLbmPsmRestart:
+    """`fix ID group lbm-psm-restart every N write 0|1 read 0|1`.
+
+    Mirrors LBMPSMWriteReadRestart (src/fix_LBM_PSM_writeReadRestart.cpp:15-78):
+    ``init`` reads this rank's restart file into the lattice when ``read 1``,
+    ``pre_force`` writes it every ``N`` timesteps when ``write 1``.  The file
+    holds the post-stream populations in the reference layout, so files of
+    the CPU code and of the GPU library are interchangeable (the halo entries
+    of periodic axes are refreshed before they are used, by either code).
+    """
+
+    def __init__(self, args: list[str], fix: FixLbmPsm, rank: int = 0, folder: str = "."):
+        narg = len(args)
+        if narg < 9:
+            raise LammpsError("Illegal fix lbm-psm-restart command")
+        self.fix = fix
+        self.nevery, self.iWrite, self.iRead = 1, 0, 0
+        self.path = os.path.join(folder, restart_file_name(rank))
+        iarg = 3
+        while iarg < narg:
+            kw = args[iarg]
+            if kw in ("every", "write", "read"):
+                if iarg + 2 > narg:
+                    raise LammpsError("Illegal fix lbm-psm-restart command")
+                try:
+                    val = int(args[iarg + 1])
+                except ValueError:
+                    raise LammpsError("Illegal fix lbm-psm-restart command")
+                if kw == "every":
+                    if val <= 0:
+                        raise LammpsError("Illegal fix lbm-psm-restart command")
+                    self.nevery = val
+                else:
+                    if val < 0 or val > 1:
+                        raise LammpsError("Illegal fix lbm-psm-restart command")
+                    setattr(self, "iWrite" if kw == "write" else "iRead", val)
+                iarg += 2
+            else:
+                raise LammpsError("Illegal fix lbm-psm-restart command")
+
+    def init(self):
+        if self.iRead == 1:
+            lat = self.fix.lattice
+            f = read_restart(self.path)
+            want = int(np.prod(lat.local)) * lat.q
+            if f.size != want:
+                raise LammpsError(f"lbm-psm-restart: {self.path} holds {f.size} values, "
+                                  f"the lattice needs {want}")
+            lat.set_populations(f)
+
+    def pre_force(self, ntimestep: int):
+        if ntimestep % self.nevery:
+            return
+        if self.iWrite == 1:
+            write_restart(self.path, self.fix.lattice.populations())
+
+
 def _fmt(v: float) -> str:
     """std::ostream default formatting of a double (6 significant digits, %g)."""
     return "%g" % v

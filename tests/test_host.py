@@ -1,7 +1,10 @@
 """Host-side mirror of the reference fixes: argument syntax and errors of
-`fix lbm-psm`, `fix lbm-psm-bc` and `fix lbm-psm-vti` (no GPU needed)."""
+`fix lbm-psm`, `fix lbm-psm-bc`, `fix lbm-psm-vti` and `fix lbm-psm-restart`,
+and the restart file layout (no GPU needed)."""
+import numpy as np
 import pytest
 
+from lbmpsm import host
 from lbmpsm.host import FixLbmPsm, FixLbmPsmBC, FixLbmPsmVTI, LammpsError, parse_fix_lbm_psm
 
 GOOD = "1 all lbm-psm every 1 Nlc 31 lc 0.0005 rho 1000.0 nu 0.0001 Re 0.1 tau 0.7".split()
@@ -50,3 +53,30 @@ def test_vti_arguments():
                 "v all lbm-psm-vti every 10 binary 2".split()):
         with pytest.raises(LammpsError, match="Illegal fix lbm-psm-vti command"):
             FixLbmPsmVTI(bad, fix)
+
+
+def test_restart_file_layout_and_arguments(tmp_path):
+    """The restart file is a native uint32 count followed by the doubles
+    (src/fix_LBM_PSM_writeReadRestart.cpp:80-103); the fix's argument rules."""
+    import struct
+
+    f = np.random.default_rng(0).normal(size=(4, 5, 3, 19))
+    path = str(tmp_path / host.restart_file_name(0))
+    host.write_restart(path, f)
+    raw = open(path, "rb").read()
+    assert raw[:4] == struct.pack("=I", f.size) and len(raw) == 4 + 8 * f.size
+    assert np.array_equal(host.read_restart(path), f.reshape(-1))
+    # a file written the reference's way reads back identically
+    ref = tmp_path / "ref.bin"
+    ref.write_bytes(struct.pack("=I", 6) + struct.pack("=6d", *range(6)))
+    assert np.array_equal(host.read_restart(str(ref)), np.arange(6.0))
+    ref.write_bytes(struct.pack("=I", 7) + struct.pack("=6d", *range(6)))
+    with pytest.raises(host.LammpsError):
+        host.read_restart(str(ref))
+    good = ["rs", "all", "lbm-psm-restart", "every", "10", "write", "1", "read", "0"]
+    fx = host.FixLbmPsmRestart(good, fix=None)
+    assert (fx.nevery, fx.iWrite, fx.iRead) == (10, 1, 0)
+    for bad in (good[:-2], good[:4] + ["0"] + good[5:], good[:6] + ["2"] + good[7:],
+                good[:7] + ["reed", "0"]):
+        with pytest.raises(host.LammpsError, match="Illegal fix lbm-psm-restart command"):
+            host.FixLbmPsmRestart(bad, fix=None)
