@@ -199,6 +199,27 @@ int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps);
 /* Copy the per-image outputs of the last step to host memory. */
 int lbmpsm_read_forces(lbmpsm_handle* h, int n, double* fh, double* th, double* stresslet);
 
+/* Batched ensemble: nbox independent lattices ("boxes") that share the
+ * lattice geometry (dimension, domain lengths, periodicity, lattice spacing)
+ * but each have their own fix parameters (tau, rho, nu, Re, Fext, boxlo),
+ * held in one allocation and advanced by one set of kernels per step (the
+ * boxes are stacked along z on the device, each wrapping within itself).
+ * One such box per LAMMPS run is what `fix lbm-psm` describes
+ * (src/fix_LBM_PSM.cpp:104-177); the ensemble has no counterpart in the
+ * reference.  Boundary conditions are not available for nbox > 1.
+ * params points to nbox structures.  A handle from lbmpsm_create is an
+ * ensemble of one box. */
+int lbmpsm_create_batch(int nbox, const lbmpsm_fix_params* params, const lbmpsm_options* opts,
+                        lbmpsm_handle** out);
+/* lbmpsm_step for an ensemble: box[i] is the box of image i, and its
+ * position is in that box's own frame.  Outputs per image as lbmpsm_step. */
+int lbmpsm_step_batch(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
+                      const double* v, const double* omega, const double* radius, double* fh,
+                      double* th, double* stresslet);
+/* The box that lbmpsm_get/set_populations, lbmpsm_export_fields and
+ * lbmpsm_get_particle_table address (default 0). */
+int lbmpsm_select_box(lbmpsm_handle* h, int box);
+
 /* Allocation-free variant of lbmpsm_export_fields; no counterpart in the
  * reference.  For callers that cannot allocate device memory while a run is
  * under way: a host program whose pool allocator already holds nearly all of

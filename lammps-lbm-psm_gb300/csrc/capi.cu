@@ -74,6 +74,14 @@ struct lbmpsm_handle {
   int graph_bc = -1;
   size_t dev_bytes = 0;
   std::string err;
+  // batched ensemble: nbox boxes stacked along z (one lattice: nbox = 1)
+  int nbox = 1;
+  std::vector<BoxParams> boxes;
+  BoxParams* d_box = nullptr;
+  int* d_img_box = nullptr;  // box of each image (cap entries)
+  bool step_boxes = false;   // the current images carry box indices
+  bool any_force = false;
+  int sel_box = 0;           // box the reference-layout calls address
 };
 
 namespace {
@@ -224,6 +232,8 @@ void free_particles(lbmpsm_handle* h) {
   dfree(h->d_xvw);
   dfree(h->d_out);
   dfree(h->d_img);
+  dfree(h->d_img_box);
+  h->d_img_box = nullptr;
   dfree(h->d_list);
   dfree(h->d_sfcode);
   dfree(h->d_shell);
@@ -270,7 +280,8 @@ int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
     CUDA_TRY(h, dmalloc(h, &h->d_xvw, sizeof(double) * 10 * cap));
     CUDA_TRY(h, dmalloc(h, &h->d_out, sizeof(double) * 12 * cap));
     CUDA_TRY(h, dmalloc(h, &h->d_img, sizeof(Img) * cap));
-    h->h_stage_bytes = (sizeof(int) + sizeof(double) * 10 + sizeof(double) * 12) * (size_t)cap + 64;
+    CUDA_TRY(h, dmalloc(h, &h->d_img_box, sizeof(int) * cap));
+    h->h_stage_bytes = (2 * sizeof(int) + sizeof(double) * 10 + sizeof(double) * 12) * (size_t)cap + 64;
     CUDA_TRY(h, cudaMallocHost(&h->h_stage, h->h_stage_bytes));
     h->cap = cap;
     h->list_cap = 0;
@@ -306,6 +317,34 @@ int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
   return LBMPSM_OK;
 }
 
+// The selected box of an ensemble seen as a lattice of its own: the same
+// strides, one box's planes, every array offset to the box's first plane.
+Geom box_geom(const lbmpsm_handle* h) {
+  Geom g = h->g;
+  g.S[2] = g.bz;
+  g.nbox = 1;
+  g.fbz = make_fastdiv((unsigned)g.bz);
+  g.N = (long long)g.P0 * g.S[1] * g.bz;
+  return g;
+}
+long long box_base(const lbmpsm_handle* h) {
+  return (long long)h->sel_box * h->g.bz * h->g.S[1] * h->g.P0;
+}
+void* box_f(const lbmpsm_handle* h) {
+  return static_cast<char*>(h->f) + box_base(h) * (long long)storage_bytes(h->opt.storage);
+}
+Table box_table(const lbmpsm_handle* h) {
+  Table t = h->tab;
+  const long long b = box_base(h);
+  t.flag += b;
+  t.ids += b;
+  if (t.eps) t.eps += b;
+  if (t.us) t.us += 6 * b;
+  if (t.rec32) t.rec32 += 2 * b;
+  t.nodeF = static_cast<char*>(t.nodeF) + 6 * b * (h->opt.storage == LBMPSM_STORAGE_FP64 ? 8 : 4);
+  return t;
+}
+
 int collide(lbmpsm_handle* h) {
   CollideParams p{};
   p.g = h->g;
@@ -315,21 +354,12 @@ int collide(lbmpsm_handle* h) {
   p.rho_out = h->rho;
   p.u_out = h->u;
   p.weighting = h->opt.psm_weighting;
-  p.tau = h->tau;
-  p.omega = h->omega;
-  p.one_minus_omega = 1.0 - h->omega;
-  p.guo_pref = (1.0 - 0.5 * h->omega);
-  for (int d = 0; d < 3; ++d) p.F[d] = h->F_lbm[d];
-  p.has_force = h->has_force ? 1 : 0;
+  p.box = h->d_box;
+  p.has_force = h->any_force ? 1 : 0;
   p.invCs2 = h->invCs2;
   p.invCs4 = h->invCs4;
   p.scale16 = h->scale16;
   p.status = h->d_status;
-  p.omega_f = (float)p.omega;
-  p.omo_f = (float)p.one_minus_omega;
-  p.gpref_f = (float)p.guo_pref;
-  p.tm_f = (float)(p.tau - 0.5);
-  for (int d = 0; d < 3; ++d) p.F_f[d] = (float)p.F[d];
   p.pipe = h->pipe;
   const int odd = (int)(h->t & 1);
   cudaError_t e;
@@ -368,12 +398,9 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     m.v = v;
     m.omega = w;
     m.radius = r;
-    for (int d = 0; d < 3; ++d) m.origin[d] = h->origin[d];
+    m.img_box = h->step_boxes ? h->d_img_box : nullptr;
+    m.box = h->d_box;
     m.dx = h->dx;
-    m.Uc = h->Uc;
-    m.u_lb = h->u_lb;
-    m.tc = h->tc;
-    m.dt_d = h->dt_d;
     m.sqrt2half = h->g.dim == 3 ? std::sqrt(3.1) / 2.0 : std::sqrt(2.1) / 2.0;
     m.img = h->d_img;
     for (int d = 0; d < 3; ++d) {
@@ -406,12 +433,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     rp.tab = h->tab;
     rp.n = n;
     rp.tag = tag;
-    rp.x = x;
-    rp.radius = r;
-    for (int d = 0; d < 3; ++d) rp.origin[d] = h->origin[d];
-    rp.dx = h->dx;
-    rp.forceFactor = h->forceFactor;
-    rp.torqueFactor = h->torqueFactor;
+    rp.box = h->d_box;
     rp.nodeF_is_double = h->opt.storage == LBMPSM_STORAGE_FP64 ? 1 : 0;
     rp.fh = h->d_out;
     rp.th = h->d_out + 3 * (size_t)n;
@@ -471,60 +493,123 @@ const char* lbmpsm_last_error(const lbmpsm_handle* h) {
   return h ? h->err.c_str() : g_create_error.c_str();
 }
 
-int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm_handle** out) {
+}  // extern "C"
+
+namespace {
+// fix_LBM_PSM constructor and init checks (src/fix_LBM_PSM.cpp:15-83,122-140)
+// and UnitConversion (src/LBM_PSM_unitConversion.cpp:15-38) of one box.
+int box_setup(const lbmpsm_fix_params* p, BoxParams& bp, double& dx, double& volumeForceFactor,
+              std::string& msg) {
+  if (p->dimension != 2 && p->dimension != 3) {
+    msg = "Illegal fix lbm-psm command: dimension must be 2 or 3";
+    return LBMPSM_ERR_ARG;
+  }
+  if (p->nevery <= 0 || p->Nlc <= 0 || !(p->lc > 0.0) || !(p->rho > 0.0) || !(p->nu > 0.0) ||
+      !(p->Re > 0.0) || !(p->tau > 0.5)) {
+    msg = "Illegal fix lbm-psm command";
+    return LBMPSM_ERR_ARG;
+  }
+  if (p->Nlc < 2) {
+    msg = "Illegal fix lbm-psm command: Nlc must be > 1";
+    return LBMPSM_ERR_ARG;
+  }
+  const double Uc_d = 1.0, Lc_d = 1.0, csPow2 = 1.0 / 3.0;
+  const int N = p->Nlc;
+  const double nu_lb = (p->tau - 0.5) * csPow2;
+  dx = p->lc / (double)(N - 1);
+  const double dx_d = Lc_d / (double)(N - 1);
+  bp.Uc = p->Re * p->nu / p->lc;
+  bp.u_lb = p->Re * nu_lb / (double)(N - 1);
+  bp.dt_d = dx_d * bp.u_lb / Uc_d;
+  bp.tc = p->lc / bp.Uc;
+  bp.forceFactor = p->rho * pow(p->lc, 4) / pow(bp.tc, 2) * pow(dx_d, 4) / pow(bp.dt_d, 2);
+  bp.torqueFactor = p->rho * pow(p->lc, 5) / pow(bp.tc, 2) * pow(dx_d, 5) / pow(bp.dt_d, 2);
+  volumeForceFactor = p->rho * p->lc / pow(bp.tc, 2) * dx_d / pow(bp.dt_d, 2);
+  const double Ma = bp.u_lb / (1.0 / sqrt(3.0));
+  if (Ma > 0.3) {
+    msg = "Mach number is Ma > 0.3. Aborting simulation. Choose parameters which give Ma < "
+          "0.3 for stability reasons.";
+    return LBMPSM_ERR_MACH;
+  }
+  const double SMALL = 1e-15;
+  if (pow(((double)((int)(p->prd[0] / dx + 0.5)) - p->prd[0] / dx), 2.0) > SMALL ||
+      pow(((double)((int)(p->prd[1] / dx + 0.5)) - p->prd[1] / dx), 2.0) > SMALL ||
+      pow(((double)((int)(p->prd[2] / dx + 0.5)) - p->prd[2] / dx), 2.0) > SMALL) {
+    msg = "Illegal cell width. Division of domain length and cell width has to give an "
+          "integer.";
+    return LBMPSM_ERR_GRID;
+  }
+  bp.origin[0] = p->boxlo[0];
+  bp.origin[1] = p->boxlo[1];
+  bp.origin[2] = p->dimension == 2 ? 0.0 : p->boxlo[2];
+  for (int d = 0; d < 3; ++d) bp.F[d] = p->Fext[d] / volumeForceFactor;
+  bp.has_force = (bp.F[0] * bp.F[0] + bp.F[1] * bp.F[1] + bp.F[2] * bp.F[2]) > 0.0 ? 1 : 0;
+  bp.tau = p->tau;
+  bp.omega = 1.0 / p->tau;
+  bp.one_minus_omega = 1.0 - bp.omega;
+  bp.guo_pref = (1.0 - 0.5 * bp.omega);
+  // FP32 copies made on the host (double->float conversions are slow on the device)
+  bp.omega_f = (float)bp.omega;
+  bp.omo_f = (float)bp.one_minus_omega;
+  bp.gpref_f = (float)bp.guo_pref;
+  bp.tm_f = (float)(bp.tau - 0.5);
+  for (int d = 0; d < 3; ++d) bp.F_f[d] = (float)bp.F[d];
+  return LBMPSM_OK;
+}
+
+int create_impl(int nbox, const lbmpsm_fix_params* ps, const lbmpsm_options* opts,
+                lbmpsm_handle** out) {
   if (!out) return fail(nullptr, LBMPSM_ERR_ARG, "out is NULL");
   *out = nullptr;
-  if (!p) return fail(nullptr, LBMPSM_ERR_ARG, "params is NULL");
-  // fix_LBM_PSM ctor checks (src/fix_LBM_PSM.cpp:15-83)
-  if (p->dimension != 2 && p->dimension != 3)
-    return fail(nullptr, LBMPSM_ERR_ARG, "Illegal fix lbm-psm command: dimension must be 2 or 3");
-  if (p->nevery <= 0 || p->Nlc <= 0 || !(p->lc > 0.0) || !(p->rho > 0.0) || !(p->nu > 0.0) ||
-      !(p->Re > 0.0) || !(p->tau > 0.5))
-    return fail(nullptr, LBMPSM_ERR_ARG, "Illegal fix lbm-psm command");
-  if (p->Nlc < 2) return fail(nullptr, LBMPSM_ERR_ARG, "Illegal fix lbm-psm command: Nlc must be > 1");
+  if (!ps) return fail(nullptr, LBMPSM_ERR_ARG, "params is NULL");
+  if (nbox < 1) return fail(nullptr, LBMPSM_ERR_ARG, "an ensemble needs at least one box");
+  const lbmpsm_fix_params* p = ps;
   lbmpsm_options o{};
   if (opts) o = *opts;
   if (o.storage < 0 || o.storage > 2)
     return fail(nullptr, LBMPSM_ERR_ARG, "unknown storage precision");
   if (o.psm_weighting < 0 || o.psm_weighting > 1)
     return fail(nullptr, LBMPSM_ERR_ARG, "unknown PSM weighting");
+  std::vector<BoxParams> boxes((size_t)nbox);
+  double dx = 0.0, vff = 0.0;
+  for (int b = 0; b < nbox; ++b) {
+    std::string msg;
+    double dxb = 0.0, vffb = 0.0;
+    const int rc = box_setup(&ps[b], boxes[(size_t)b], dxb, vffb, msg);
+    if (rc) return fail(nullptr, rc, nbox > 1 ? "box " + std::to_string(b) + ": " + msg : msg);
+    if (b == 0) {
+      dx = dxb;
+      vff = vffb;
+      continue;
+    }
+    // one lattice geometry for every box of an ensemble
+    const lbmpsm_fix_params& q = ps[b];
+    bool same = q.dimension == p->dimension && dxb == dx;
+    for (int d = 0; d < 3; ++d)
+      same = same && q.prd[d] == p->prd[d] && (q.periodic[d] != 0) == (p->periodic[d] != 0);
+    if (!same)
+      return fail(nullptr, LBMPSM_ERR_ARG,
+                  "box " + std::to_string(b) + ": the boxes of an ensemble must share dimension, "
+                  "domain lengths, periodicity and lattice spacing");
+  }
 
   lbmpsm_handle* h = new (std::nothrow) lbmpsm_handle();
   if (!h) return fail(nullptr, LBMPSM_ERR_NOMEM, "host allocation failed");
   h->prm = *p;
   h->opt = o;
-  // UnitConversion::UnitConversion (src/LBM_PSM_unitConversion.cpp:15-38)
-  {
-    const double Uc_d = 1.0, Lc_d = 1.0, csPow2 = 1.0 / 3.0;
-    const int N = p->Nlc;
-    h->nu_lb = (p->tau - 0.5) * csPow2;
-    h->dx = p->lc / (double)(N - 1);
-    h->dx_d = Lc_d / (double)(N - 1);
-    h->Uc = p->Re * p->nu / p->lc;
-    h->u_lb = p->Re * h->nu_lb / (double)(N - 1);
-    h->dt_d = h->dx_d * h->u_lb / Uc_d;
-    h->tc = p->lc / h->Uc;
-    h->forceFactor = p->rho * pow(p->lc, 4) / pow(h->tc, 2) * pow(h->dx_d, 4) / pow(h->dt_d, 2);
-    h->torqueFactor = p->rho * pow(p->lc, 5) / pow(h->tc, 2) * pow(h->dx_d, 5) / pow(h->dt_d, 2);
-    h->volumeForceFactor = p->rho * p->lc / pow(h->tc, 2) * h->dx_d / pow(h->dt_d, 2);
-  }
-  // fix_LBM_PSM::init checks (src/fix_LBM_PSM.cpp:122-140)
-  const double Ma = h->u_lb / (1.0 / sqrt(3.0));
-  if (Ma > 0.3) {
-    delete h;
-    return fail(nullptr, LBMPSM_ERR_MACH,
-                "Mach number is Ma > 0.3. Aborting simulation. Choose parameters which give Ma < "
-                "0.3 for stability reasons.");
-  }
-  const double SMALL = 1e-15, dx = h->dx;
-  if (pow(((double)((int)(p->prd[0] / dx + 0.5)) - p->prd[0] / dx), 2.0) > SMALL ||
-      pow(((double)((int)(p->prd[1] / dx + 0.5)) - p->prd[1] / dx), 2.0) > SMALL ||
-      pow(((double)((int)(p->prd[2] / dx + 0.5)) - p->prd[2] / dx), 2.0) > SMALL) {
-    delete h;
-    return fail(nullptr, LBMPSM_ERR_GRID,
-                "Illegal cell width. Division of domain length and cell width has to give an "
-                "integer.");
-  }
+  h->nbox = nbox;
+  h->boxes = boxes;
+  const BoxParams& b0 = boxes[0];
+  h->dx = dx;
+  h->dx_d = 1.0 / (double)(p->Nlc - 1);
+  h->nu_lb = (p->tau - 0.5) / 3.0;
+  h->Uc = b0.Uc;
+  h->u_lb = b0.u_lb;
+  h->dt_d = b0.dt_d;
+  h->tc = b0.tc;
+  h->forceFactor = b0.forceFactor;
+  h->torqueFactor = b0.torqueFactor;
+  h->volumeForceFactor = vff;
   int gn[3];
   gn[0] = p->prd[0] / dx + 1.5;
   if (p->periodic[0]) gn[0] -= 1;
@@ -540,11 +625,11 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
       delete h;
       return fail(nullptr, LBMPSM_ERR_GRID, "lattice has no nodes along an axis");
     }
-  h->origin[0] = p->boxlo[0];
-  h->origin[1] = p->boxlo[1];
-  h->origin[2] = p->dimension == 2 ? 0.0 : p->boxlo[2];
-  for (int d = 0; d < 3; ++d) h->F_lbm[d] = p->Fext[d] / h->volumeForceFactor;
-  h->has_force = (h->F_lbm[0] * h->F_lbm[0] + h->F_lbm[1] * h->F_lbm[1] + h->F_lbm[2] * h->F_lbm[2]) > 0.0;
+  for (int d = 0; d < 3; ++d) h->origin[d] = b0.origin[d];
+  for (int d = 0; d < 3; ++d) h->F_lbm[d] = b0.F[d];
+  h->has_force = b0.has_force != 0;
+  h->any_force = false;
+  for (const BoxParams& bp : boxes) h->any_force = h->any_force || bp.has_force;
   h->tau = p->tau;
   h->omega = 1.0 / p->tau;
   {
@@ -562,6 +647,14 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
     g.per[d] = per ? 1 : 0;
     g.off[d] = (real_axis && per) ? 1 : 0;
     g.S[d] = (real_axis && per) ? gn[d] : g.L[d];
+  }
+  g.bz = g.S[2];
+  g.nbox = nbox;
+  g.fbz = make_fastdiv((unsigned)g.bz);
+  g.S[2] = g.bz * nbox;
+  if ((long long)g.S[2] > 65535 || g.L[0] > 65535 || g.L[1] > 65535) {
+    delete h;
+    return fail(nullptr, LBMPSM_ERR_GRID, "more than 65535 nodes along an axis");
   }
   g.P0 = (g.S[0] + 7) / 8 * 8;
   g.N = (long long)g.P0 * g.S[1] * g.S[2];
@@ -615,6 +708,11 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
         cudaMemcpy(h->d_sf_value32, tbl32, sizeof(tbl32), cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(LBMPSM_ERR_CUDA);
   }
+  if (dmalloc(h, &h->d_box, sizeof(BoxParams) * (size_t)nbox) != cudaSuccess)
+    return bail(LBMPSM_ERR_NOMEM);
+  if (cudaMemcpy(h->d_box, h->boxes.data(), sizeof(BoxParams) * (size_t)nbox,
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(LBMPSM_ERR_CUDA);
   cudaMemsetAsync(h->tab.flag, 0, N, h->stream);
   cudaMemsetAsync(h->tab.ids, 0, sizeof(int2) * N, h->stream);
   if (h->tab.eps) cudaMemsetAsync(h->tab.eps, 0, sizeof(double2) * N, h->stream);
@@ -645,6 +743,18 @@ int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm
   *out = h;
   return LBMPSM_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int lbmpsm_create(const lbmpsm_fix_params* p, const lbmpsm_options* opts, lbmpsm_handle** out) {
+  return create_impl(1, p, opts, out);
+}
+
+int lbmpsm_create_batch(int nbox, const lbmpsm_fix_params* params, const lbmpsm_options* opts,
+                        lbmpsm_handle** out) {
+  return create_impl(nbox, params, opts, out);
+}
 
 void lbmpsm_destroy(lbmpsm_handle* h) {
   if (!h) return;
@@ -667,6 +777,7 @@ void lbmpsm_destroy(lbmpsm_handle* h) {
   dfree(h->d_check);
   dfree(h->d_sf_value);
   dfree(h->d_sf_value32);
+  dfree(h->d_box);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -698,8 +809,17 @@ int lbmpsm_get_info(const lbmpsm_handle* h, lbmpsm_info* info) {
   return LBMPSM_OK;
 }
 
+int lbmpsm_select_box(lbmpsm_handle* h, int box) {
+  if (!h) return LBMPSM_ERR_ARG;
+  if (box < 0 || box >= h->nbox) return fail(h, LBMPSM_ERR_ARG, "box index out of range");
+  h->sel_box = box;
+  return LBMPSM_OK;
+}
+
 int lbmpsm_set_bc(lbmpsm_handle* h, int bc_type) {
   if (!h) return LBMPSM_ERR_ARG;
+  if (h->nbox > 1 && bc_type != LBMPSM_BC_NONE)
+    return fail(h, LBMPSM_ERR_STATE, "boundary conditions need a lattice of one box");
   if (bc_type < 0 || bc_type > 5) return fail(h, LBMPSM_ERR_ARG, "Illegal fix lbm-psm-bc command");
   h->bc_type = bc_type;
   make_faces(h, bc_type);
@@ -707,12 +827,23 @@ int lbmpsm_set_bc(lbmpsm_handle* h, int bc_type) {
   return LBMPSM_OK;
 }
 
-int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
-                const double* omega, const double* radius, double* fh, double* th,
-                double* stresslet) {
+}  // extern "C"
+
+namespace {
+// one coupling step with host arrays; box (may be null) gives each image's box
+int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
+              const double* v, const double* omega, const double* radius, double* fh, double* th,
+              double* stresslet) {
   if (!h || n < 0) return LBMPSM_ERR_ARG;
   if (n > 0 && (!tag || !x || !v || !omega || !radius || !fh || !th || !stresslet))
     return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
+  if (box) {
+    for (int i = 0; i < n; ++i)
+      if (box[i] < 0 || box[i] >= h->nbox)
+        return fail(h, LBMPSM_ERR_ARG, "image " + std::to_string(i) + ": box index out of range");
+  } else if (h->nbox > 1 && n > 0) {
+    return fail(h, LBMPSM_ERR_ARG, "an ensemble needs the box of every image (lbmpsm_step_batch)");
+  }
   CUDA_TRY(h, cudaSetDevice(h->device));
   double rmax = 0.0;
   for (int i = 0; i < n; ++i) rmax = std::max(rmax, radius[i]);
@@ -720,12 +851,17 @@ int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
     return fail(h, LBMPSM_ERR_NUMERIC, "non-finite particle position or radius");
   int rc = ensure_particles(h, n, std::max(rmax, h->opt.max_radius));
   if (rc) return rc;
+  // pinned staging: tags | boxes | x | v | omega | radius | outputs
+  const size_t cap = (size_t)h->cap;
+  char* st = static_cast<char*>(h->h_stage);
+  const size_t iblk = (sizeof(int) * cap + 15) & ~(size_t)15;
+  int* stag = reinterpret_cast<int*>(st);
+  int* sbox = reinterpret_cast<int*>(st + iblk);
+  double* sx = reinterpret_cast<double*>(st + 2 * iblk);
+  double* out = sx + 10 * cap;
+  if (h->step_boxes != (box != nullptr)) drop_graphs(h);  // the map reads the boxes or not
+  h->step_boxes = box != nullptr;
   if (n > 0) {
-    // pinned staging: tags, then x | v | omega | radius; two copies to the device
-    const size_t cap = (size_t)h->cap;
-    char* st = static_cast<char*>(h->h_stage);
-    int* stag = reinterpret_cast<int*>(st);
-    double* sx = reinterpret_cast<double*>(st + ((sizeof(int) * cap + 15) & ~(size_t)15));
     const size_t nn = (size_t)n;
     std::memcpy(stag, tag, sizeof(int) * nn);
     std::memcpy(sx, x, sizeof(double) * 3 * nn);
@@ -733,15 +869,17 @@ int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
     std::memcpy(sx + 6 * nn, omega, sizeof(double) * 3 * nn);
     std::memcpy(sx + 9 * nn, radius, sizeof(double) * nn);
     CUDA_TRY(h, cudaMemcpyAsync(h->d_tag, stag, sizeof(int) * nn, cudaMemcpyHostToDevice, h->stream));
+    if (box) {
+      std::memcpy(sbox, box, sizeof(int) * nn);
+      CUDA_TRY(h, cudaMemcpyAsync(h->d_img_box, sbox, sizeof(int) * nn, cudaMemcpyHostToDevice,
+                                  h->stream));
+    }
     CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw, sx, sizeof(double) * 10 * nn, cudaMemcpyHostToDevice,
                                 h->stream));
   }
   rc = enqueue_step(h, n);
   if (rc) return rc;
   if (n > 0) {
-    double* out = reinterpret_cast<double*>(static_cast<char*>(h->h_stage) +
-                                            ((sizeof(int) * h->cap + 15) & ~(size_t)15) +
-                                            sizeof(double) * 10 * (size_t)h->cap);
     CUDA_TRY(h, cudaMemcpyAsync(out, h->d_out, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost,
                                 h->stream));
     rc = read_status(h);  // synchronises
@@ -754,6 +892,22 @@ int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
   }
   return LBMPSM_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
+                const double* omega, const double* radius, double* fh, double* th,
+                double* stresslet) {
+  return step_impl(h, n, nullptr, tag, x, v, omega, radius, fh, th, stresslet);
+}
+
+int lbmpsm_step_batch(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
+                      const double* v, const double* omega, const double* radius, double* fh,
+                      double* th, double* stresslet) {
+  if (n > 0 && !box) return fail(h, LBMPSM_ERR_ARG, "NULL box array");
+  return step_impl(h, n, box, tag, x, v, omega, radius, fh, th, stresslet);
+}
 
 int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
                        const double* omega, const double* radius, double* fh, double* th,
@@ -762,7 +916,11 @@ int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
   if (n > h->cap) return fail(h, LBMPSM_ERR_CAPACITY, "more images than options.max_images");
   if (h->opt.max_radius <= 0.0)
     return fail(h, LBMPSM_ERR_ARG, "lbmpsm_step_device needs options.max_radius");
+  if (h->nbox > 1 && n > 0)
+    return fail(h, LBMPSM_ERR_ARG, "an ensemble needs the box of every image (lbmpsm_step_batch)");
   CUDA_TRY(h, cudaSetDevice(h->device));
+  if (h->step_boxes) drop_graphs(h);
+  h->step_boxes = false;
   const size_t nn = (size_t)n;
   if (n > 0) {
     CUDA_TRY(h, cudaMemcpyAsync(h->d_tag, tag, sizeof(int) * nn, cudaMemcpyDeviceToDevice, h->stream));
@@ -803,15 +961,16 @@ int lbmpsm_export_fields(lbmpsm_handle* h, int as_double, double B0, double rho0
                          void* solid, void* rho, void* u) {
   if (!h) return LBMPSM_ERR_ARG;
   CUDA_TRY(h, cudaSetDevice(h->device));
-  const Geom& g = h->g;
+  const Geom g = box_geom(h);
+  const long long base = box_base(h);
   const size_t npts = (size_t)(g.L[0] - 2) * (g.L[1] - 2) * (g.dim == 3 ? g.L[2] - 2 : 1);
   const size_t es = as_double ? 8 : 4;
   void* d = nullptr;
   CUDA_TRY(h, cudaMalloc(&d, es * 5 * npts));
   char* b = static_cast<char*>(d);
-  cudaError_t e = launch_export_fields(g, h->tab, h->macro_valid ? h->rho : nullptr,
-                                       h->macro_valid ? h->u : nullptr, as_double, B0, rho0, u0, b,
-                                       b + es * npts, b + 2 * es * npts, h->stream);
+  cudaError_t e = launch_export_fields(g, box_table(h), h->macro_valid ? h->rho + base : nullptr,
+                                       h->macro_valid ? h->u + 3 * base : nullptr, as_double, B0,
+                                       rho0, u0, b, b + es * npts, b + 2 * es * npts, h->stream);
   if (e == cudaSuccess && solid) e = cudaMemcpyAsync(solid, b, es * npts, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess && rho) e = cudaMemcpyAsync(rho, b + es * npts, es * npts, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, b + 2 * es * npts, 3 * es * npts, cudaMemcpyDeviceToHost, h->stream);
@@ -824,11 +983,11 @@ int lbmpsm_export_fields(lbmpsm_handle* h, int as_double, double B0, double rho0
 int lbmpsm_get_populations(lbmpsm_handle* h, double* f) {
   if (!h || !f) return LBMPSM_ERR_ARG;
   CUDA_TRY(h, cudaSetDevice(h->device));
-  const Geom& g = h->g;
+  const Geom g = box_geom(h);
   const size_t cnt = (size_t)g.L[0] * g.L[1] * g.L[2] * g.Q;
   double* d = nullptr;
   CUDA_TRY(h, cudaMalloc(&d, sizeof(double) * cnt));
-  cudaError_t e = launch_get_populations(g, h->f, h->opt.storage, (h->t % 2 == 0) ? 1 : 0,
+  cudaError_t e = launch_get_populations(g, box_f(h), h->opt.storage, (h->t % 2 == 0) ? 1 : 0,
                                          h->scale16, d, h->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(f, d, sizeof(double) * cnt, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -840,14 +999,14 @@ int lbmpsm_get_populations(lbmpsm_handle* h, double* f) {
 int lbmpsm_set_populations(lbmpsm_handle* h, const double* f) {
   if (!h || !f) return LBMPSM_ERR_ARG;
   CUDA_TRY(h, cudaSetDevice(h->device));
-  const Geom& g = h->g;
+  const Geom g = box_geom(h);
   const size_t cnt = (size_t)g.L[0] * g.L[1] * g.L[2] * g.Q;
   double* d = nullptr;
   CUDA_TRY(h, cudaMalloc(&d, sizeof(double) * cnt));
   cudaError_t e = cudaMemcpyAsync(d, f, sizeof(double) * cnt, cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess)
-    e = launch_set_populations(g, h->f, h->opt.storage, (h->t % 2 == 0) ? 1 : 0, h->scale16, d,
-                               h->stream);
+    e = launch_set_populations(g, box_f(h), h->opt.storage, (h->t % 2 == 0) ? 1 : 0, h->scale16,
+                               d, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   cudaFree(d);
   CUDA_TRY(h, e);
@@ -857,14 +1016,14 @@ int lbmpsm_set_populations(lbmpsm_handle* h, const double* f) {
 int lbmpsm_get_particle_table(lbmpsm_handle* h, int* ids, double* eps, double* us) {
   if (!h) return LBMPSM_ERR_ARG;
   CUDA_TRY(h, cudaSetDevice(h->device));
-  const Geom& g = h->g;
+  const Geom g = box_geom(h);
   const size_t N = (size_t)g.L[0] * g.L[1] * g.L[2];
   void* d = nullptr;
   CUDA_TRY(h, cudaMalloc(&d, N * (2 * sizeof(int) + 8 * sizeof(double))));
   int* di = static_cast<int*>(d);
   double* de = reinterpret_cast<double*>(di + 2 * N);
   double* du = de + 2 * N;
-  cudaError_t e = launch_table_export(g, h->tab, di, de, du, h->stream);
+  cudaError_t e = launch_table_export(g, box_table(h), di, de, du, h->stream);
   if (e == cudaSuccess && ids) e = cudaMemcpyAsync(ids, di, sizeof(int) * 2 * N, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess && eps) e = cudaMemcpyAsync(eps, de, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess && us) e = cudaMemcpyAsync(us, du, sizeof(double) * 6 * N, cudaMemcpyDeviceToHost, h->stream);

@@ -59,7 +59,7 @@ struct PsmNode {
 template <class L, int q>
 __device__ __forceinline__ void collide_q(double& fq, double rho, double ux, double uy,
                                           double uz, double usq_half, const CollideParams& p,
-                                          bool psm, PsmNode& sn) {
+                                          const BoxParams& bp, bool psm, PsmNode& sn) {
   constexpr int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
   const double w = L::w(q);
   const double fi = fq;
@@ -68,14 +68,14 @@ __device__ __forceinline__ void collide_q(double& fq, double rho, double ux, dou
   const double fi_eq = rho * w * (1.0 + eu * p.invCs2 + eu * eu * 0.5 * p.invCs4 - usq_half);
   // Guo forcing (src/LBM_PSM_dynamics.h:102-116), scaled by (1 - omega/2)
   double Fq = 0.0;
-  if (p.has_force) {
-    const double a = ((double)cx - ux) * p.F[0] + ((double)cy - uy) * p.F[1] +
-                     ((double)cz - uz) * p.F[2];
-    const double eF = (q == 0) ? 0.0 : edot<cx, cy, cz>(p.F[0], p.F[1], p.F[2]);
-    Fq = p.guo_pref * (w * (a * p.invCs2 + (eu * p.invCs4 * eF)));
+  if (bp.has_force) {
+    const double a = ((double)cx - ux) * bp.F[0] + ((double)cy - uy) * bp.F[1] +
+                     ((double)cz - uz) * bp.F[2];
+    const double eF = (q == 0) ? 0.0 : edot<cx, cy, cz>(bp.F[0], bp.F[1], bp.F[2]);
+    Fq = bp.guo_pref * (w * (a * p.invCs2 + (eu * p.invCs4 * eF)));
   }
   if (!psm) {
-    fq = fi + (fi_eq - fi) * p.omega + Fq;
+    fq = fi + (fi_eq - fi) * bp.omega + Fq;
     return;
   }
   double sc1 = 0.0, sc2 = 0.0;
@@ -83,14 +83,14 @@ __device__ __forceinline__ void collide_q(double& fq, double rho, double ux, dou
     // feq(iq, rho, uSolid) array overload (src/LBM_PSM_dynamics.h:72-85)
     const double eus = (q == 0) ? 0.0 : edot<cx, cy, cz>(sn.us1[0], sn.us1[1], sn.us1[2]);
     const double f0s = rho * w * (1.0 + eus * p.invCs2 + 0.5 * eus * eus * p.invCs4 - sn.half1);
-    sc1 = f0s - fi + p.one_minus_omega * (fi - fi_eq);
+    sc1 = f0s - fi + bp.one_minus_omega * (fi - fi_eq);
   }
   if (sn.has2) {
     const double eus = (q == 0) ? 0.0 : edot<cx, cy, cz>(sn.us2[0], sn.us2[1], sn.us2[2]);
     const double f0s = rho * w * (1.0 + eus * p.invCs2 + 0.5 * eus * eus * p.invCs4 - sn.half2);
-    sc2 = f0s - fi + p.one_minus_omega * (fi - fi_eq);
+    sc2 = f0s - fi + bp.one_minus_omega * (fi - fi_eq);
   }
-  fq = fi + sn.oneMinusBtot * (fi_eq - fi) * p.omega + sn.B1 * sc1 + sn.B2 * sc2 + Fq;
+  fq = fi + sn.oneMinusBtot * (fi_eq - fi) * bp.omega + sn.B1 * sc1 + sn.B2 * sc2 + Fq;
   // node force on the particles (add_Fhyd): F += -B*Omega_s*e
   if (sn.has1) {
     const double t = -sn.B1 * sc1;
@@ -110,15 +110,17 @@ template <class L, int q>
 struct CollideUnroll {
   __device__ __forceinline__ static void run(double* f, double rho, double ux, double uy,
                                              double uz, double usq_half,
-                                             const CollideParams& p, bool psm, PsmNode& sn) {
-    collide_q<L, q>(f[q], rho, ux, uy, uz, usq_half, p, psm, sn);
-    CollideUnroll<L, q + 1>::run(f, rho, ux, uy, uz, usq_half, p, psm, sn);
+                                             const CollideParams& p, const BoxParams& bp, bool psm,
+                                             PsmNode& sn) {
+    collide_q<L, q>(f[q], rho, ux, uy, uz, usq_half, p, bp, psm, sn);
+    CollideUnroll<L, q + 1>::run(f, rho, ux, uy, uz, usq_half, p, bp, psm, sn);
   }
 };
 template <class L>
 struct CollideUnroll<L, L::Q> {
   __device__ __forceinline__ static void run(double*, double, double, double, double, double,
-                                             const CollideParams&, bool, PsmNode&) {}
+                                             const CollideParams&, const BoxParams&, bool,
+                                             PsmNode&) {}
 };
 
 template <class L, bool ODD>
@@ -134,6 +136,7 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
   const int sz = row / g.S[1];
   const long long n = node_index(g, sx, sy, sz);
   const Nbr nb = make_nbr(g, sx, sy, sz);
+  const BoxParams& bp = p.box[box_of_z(g, sz)];
   double* __restrict__ F = static_cast<double*>(p.f);
   const long long Np = g.Np;
 
@@ -163,9 +166,9 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
     if (cy) jy = cy > 0 ? jy + f[q] : jy - f[q];
     if (cz) jz = cz > 0 ? jz + f[q] : jz - f[q];
   }
-  jx = jx + p.F[0] * 0.5;
-  jy = jy + p.F[1] * 0.5;
-  jz = jz + p.F[2] * 0.5;
+  jx = jx + bp.F[0] * 0.5;
+  jy = jy + bp.F[1] * 0.5;
+  jz = jz + bp.F[2] * 0.5;
   const double ux = jx / rho, uy = jy / rho, uz = jz / rho;
   if (p.store_macro) {
     p.rho_out[n] = rho;
@@ -187,7 +190,7 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
     double B1 = sn.has1 ? e.x : 0.0;
     double B2 = sn.has2 ? e.y : 0.0;
     if (p.weighting == 1) {  // Noble-Torczynski weighting (opt-in)
-      const double tm = p.tau - 0.5;
+      const double tm = bp.tau - 0.5;
       if (sn.has1) B1 = B1 * tm / ((1.0 - B1) + tm);
       if (sn.has2) B2 = B2 * tm / ((1.0 - B2) + tm);
     }
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
     }
   }
 
-  CollideUnroll<L, 0>::run(f, rho, ux, uy, uz, usq_half, p, psm, sn);
+  CollideUnroll<L, 0>::run(f, rho, ux, uy, uz, usq_half, p, bp, psm, sn);
 
   if (psm) {
     double* nf = static_cast<double*>(p.tab.nodeF) + 6 * n;

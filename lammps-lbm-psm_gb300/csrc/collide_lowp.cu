@@ -65,8 +65,8 @@ __device__ __forceinline__ float edot(int cx, int cy, int cz, float vx, float vy
 // an unused slot has B = 0 and leaves f' bit-identical to the shorter loop.
 template <class L, bool FORCE>
 __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const CollideParams& p,
-                                                  long long n, uint8_t flag, float4 r1,
-                                                  float4 r2) {
+                                                  const BoxParams& bp, long long n, uint8_t flag,
+                                                  float4 r1, float4 r2) {
   constexpr int Q = L::Q;
   float drho = -0.0f, jx = -0.0f, jy = -0.0f, jz = -0.0f;
 #pragma unroll
@@ -76,7 +76,7 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
     jy = sgn_add(jy, L::ey(q), f[q]);
     jz = sgn_add(jz, L::ez(q), f[q]);
   }
-  const float Fx = p.F_f[0], Fy = p.F_f[1], Fz = p.F_f[2];
+  const float Fx = bp.F_f[0], Fy = bp.F_f[1], Fz = bp.F_f[2];
   if (FORCE) {
     jx += 0.5f * Fx;
     jy += 0.5f * Fy;
@@ -92,8 +92,8 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
     p.u_out[3 * n + 2] = uz;
   }
   const float usq15 = 1.5f * (ux * ux + uy * uy + uz * uz);
-  const float omega = p.omega_f;
-  const float gpref = p.gpref_f;
+  const float omega = bp.omega_f;
+  const float gpref = bp.gpref_f;
   const float uF = FORCE ? ux * Fx + uy * Fy + uz * Fz : 0.0f;
   const float dr_u = drho - rho * usq15;
 
@@ -123,7 +123,7 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
   float B1 = has1 ? r1.x : 0.0f;
   float B2 = has2 ? r2.x : 0.0f;
   if (p.weighting == 1) {  // Noble-Torczynski weighting (opt-in)
-    const float tm = p.tm_f;
+    const float tm = bp.tm_f;
     if (has1) B1 = B1 * tm / ((1.0f - B1) + tm);
     if (has2) B2 = B2 * tm / ((1.0f - B2) + tm);
   }
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
     r1 = p.tab.rec32[2 * n];
     r2 = p.tab.rec32[2 * n + 1];
   }
-  collide_node_lowp<L, FORCE>(f, p, n, flag, r1, r2);
+  collide_node_lowp<L, FORCE>(f, p, p.box[box_of_z(g, sz)], n, flag, r1, r2);
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
@@ -274,31 +274,34 @@ constexpr int STAGED_MAX_ROW = 256;      // nodes per x-row handled by one stage
 constexpr long long MBAR_SPIN_LIMIT = 1ll << 26;
 
 // neighbour row (dy, dz) of row (sy, sz); false when it does not exist
+// (z wraps or ends within the row's box of a batched ensemble)
 __device__ __forceinline__ bool row_of(const Geom& g, int sy, int sz, int dy, int dz,
                                        long long& base) {
-  int y = sy + dy, z = sz + dz;
+  const int z0 = box_of_z(g, sz) * g.bz;
+  int y = sy + dy, z = sz - z0 + dz;
   if (y < 0 || y >= g.S[1]) {
     if (!g.per[1]) return false;
     y = y < 0 ? y + g.S[1] : y - g.S[1];
   }
-  if (z < 0 || z >= g.S[2]) {
+  if (z < 0 || z >= g.bz) {
     if (!g.per[2]) return false;
-    z = z < 0 ? z + g.S[2] : z - g.S[2];
+    z = z < 0 ? z + g.bz : z - g.bz;
   }
-  base = ((long long)z * g.S[1] + y) * g.P0;
+  base = ((long long)(z0 + z) * g.S[1] + y) * g.P0;
   return true;
 }
 
 // bit (dy+1)*3 + (dz+1) set when row (sy+dy, sz+dz) exists
 __device__ __forceinline__ unsigned row_mask(const Geom& g, int sy, int sz) {
   unsigned m = 0;
+  const int lz = sz - box_of_z(g, sz) * g.bz;  // plane within the box
 #pragma unroll
   for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
     for (int dz = -1; dz <= 1; ++dz) {
-      const int y = sy + dy, z = sz + dz;
+      const int y = sy + dy, z = lz + dz;
       const bool oky = (y >= 0 && y < g.S[1]) || g.per[1];
-      const bool okz = (z >= 0 && z < g.S[2]) || g.per[2];
+      const bool okz = (z >= 0 && z < g.bz) || g.per[2];
       if (oky && okz) m |= 1u << ((dy + 1) * 3 + (dz + 1));
     }
   return m;
@@ -518,7 +521,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
           f[q] = okq ? Store<T>::load(buf + q * P0 + xs, sc) : 0.0f;
         }
       }
-      collide_node_lowp<L, FORCE>(f, p, n, flag, r1, r2);
+      collide_node_lowp<L, FORCE>(f, p, p.box[box_of_z(g, cz)], n, flag, r1, r2);
     }
     // odd step: every input read before any output lands on a neighbour's
     // column (the even step reads and writes only the thread's own column)

@@ -71,6 +71,29 @@ struct D3Q19 {
   }
 };
 
+// Exact small-integer to float conversion without the conversion unit:
+// valid for |k| < 2^22.
+__device__ __forceinline__ float small_int_to_float(int k) {
+  return __int_as_float(0x4B400000 + k) - 12582912.0f;
+}
+
+// Division by a runtime divisor without the conversion unit (integer
+// division otherwise goes through int/float conversions, which share the slow
+// FP64 pipe on this GPU): q = umulhi(n, ceil(2^32/d)), exact for n*d < 2^32
+// (checked exhaustively for d <= 4096, n < 2^22).
+struct FastDiv {
+  unsigned d, m;
+};
+__host__ __device__ __forceinline__ FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  f.d = d;
+  f.m = d > 1 ? 0xFFFFFFFFu / d + 1u : 0u;
+  return f;
+}
+__device__ __forceinline__ unsigned fast_div(unsigned n, const FastDiv& f) {
+  return f.d > 1 ? __umulhi(n, f.m) : n;
+}
+
 // ---------------------------------------------------------------- geometry
 struct Geom {
   int dim, Q;
@@ -81,7 +104,17 @@ struct Geom {
   int P0;      // x pitch: S0 rounded up to 8 so that every x-row starts 16-byte aligned
   long long N; // P0*S1*S2 (node slots including the x padding)
   long long Np;// population stride (N rounded up to 64)
+  // A batched ensemble stacks nbox boxes of equal geometry along z: box b
+  // holds storage planes [b*bz, (b+1)*bz) and its z axis wraps (or ends)
+  // within them.  One lattice is a batch of one box (bz = S[2]).
+  int bz, nbox;
+  FastDiv fbz;
 };
+
+// box of storage plane sz and its plane within the box
+__device__ __forceinline__ int box_of_z(const Geom& g, int sz) {
+  return g.nbox > 1 ? (int)fast_div((unsigned)sz, g.fbz) : 0;
+}
 
 __host__ __device__ __forceinline__ long long node_index(const Geom& g, int sx, int sy, int sz) {
   return ((long long)sz * g.S[1] + sy) * g.P0 + sx;
@@ -97,11 +130,11 @@ struct Nbr {
 __device__ __forceinline__ Nbr make_nbr(const Geom& g, int sx, int sy, int sz) {
   Nbr nb;
   nb.v = 0;
-  const int s[3] = {sx, sy, sz};
+  const int s[3] = {sx, sy, sz - box_of_z(g, sz) * g.bz};  // z within its box
   const int stride[3] = {1, g.P0, g.P0 * g.S[1]};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const int n = g.S[a];
+    const int n = a == 2 ? g.bz : g.S[a];
     // towards -1
     if (s[a] > 0) {
       nb.o[a][0] = -stride[a];
@@ -153,6 +186,19 @@ struct Table {
 };
 
 // ---------------------------------------------------------------- step params
+// Parameters that differ between the boxes of a batched ensemble (for one
+// lattice: its own parameters).
+struct BoxParams {
+  double omega, one_minus_omega, guo_pref, tau;  // BGK / Guo, FP64
+  double F[3];                                   // F_lbm
+  float omega_f, omo_f, gpref_f, tm_f;           // FP32 copies made on the host
+  float F_f[3];
+  int has_force;                                 // |F_lbm|^2 > 0
+  double origin[3];                              // the box's own frame
+  double Uc, u_lb, tc, dt_d;                     // UnitConversion
+  double forceFactor, torqueFactor;
+};
+
 // launch shape of the row-pipelined FP32/FP16 collide kernel (grid 0: the
 // direct kernel instead)
 struct PipeConfig {
@@ -169,40 +215,14 @@ struct CollideParams {
   double* u_out;          // optional (3N)
   int store_macro;
   int weighting;          // LBMPSM_WEIGHT_*
-  double tau, omega, one_minus_omega, guo_pref;
-  double F[3];
-  int has_force;          // |F_lbm|^2 > 0
+  const BoxParams* box;   // per-box BGK / Guo parameters (g.nbox entries)
+  int has_force;          // any box with |F_lbm|^2 > 0
   double invCs2, invCs4;
   float scale16;          // FP16 storage: stored value = deviation * scale16
   int* status;            // error word (STATUS_*)
-  // FP32 copies made on the host (double->float conversions are slow on the device)
-  float omega_f, omo_f, gpref_f, tm_f;
-  float F_f[3];
   PipeConfig pipe;
 };
 
-// Exact small-integer to float conversion without the conversion unit:
-// valid for |k| < 2^22.
-__device__ __forceinline__ float small_int_to_float(int k) {
-  return __int_as_float(0x4B400000 + k) - 12582912.0f;
-}
-
-// Division by a runtime divisor without the conversion unit (integer
-// division otherwise goes through int/float conversions, which share the slow
-// FP64 pipe on this GPU): q = umulhi(n, ceil(2^32/d)), exact for n*d < 2^32
-// (checked exhaustively for d <= 4096, n < 2^22).
-struct FastDiv {
-  unsigned d, m;
-};
-__host__ __device__ __forceinline__ FastDiv make_fastdiv(unsigned d) {
-  FastDiv f;
-  f.d = d;
-  f.m = d > 1 ? 0xFFFFFFFFu / d + 1u : 0u;
-  return f;
-}
-__device__ __forceinline__ unsigned fast_div(unsigned n, const FastDiv& f) {
-  return f.d > 1 ? __umulhi(n, f.m) : n;
-}
 
 // Zou-He face list of one `fix lbm-psm-bc` keyword.
 enum FaceKind {
@@ -249,6 +269,8 @@ struct Img {
   float uTf[3], omf[3];  // FP32 roundings of uT and om (FP32 / FP16 storage)
   int solo;           // no periodic copy of the particle can have an overlapping box
   int qlo[3], qhi[3]; // part of the reduction box the reduction visits
+  int bidx;           // box of a batched ensemble (0 for one lattice)
+  int zoff;           // its first storage plane (bidx * bz); lo/hi above are global
 };
 
 // Solid-fraction codes of one (image, node) pair: 0..1000 = number of
@@ -264,8 +286,9 @@ struct MapParams {
   const double* v;
   const double* omega;
   const double* radius;
-  double origin[3];
-  double dx, Uc, u_lb, tc, dt_d;
+  const int* img_box;  // box of each image (batched ensemble) or null (all box 0)
+  const BoxParams* box;
+  double dx;
   double sqrt2half;   // sqrt(2.1)/2 in 2-D, sqrt(3.1)/2 in 3-D (host libm)
   Img* img;
   int cb[3];          // cell edge (nodes) per axis
@@ -291,13 +314,9 @@ struct ReduceParams {
   Geom g;
   Table tab;
   const Img* img;     // image records of the step's map (centre, box)
+  const BoxParams* box;
   int n;
   const int* tag;
-  const double* x;
-  const double* radius;
-  double origin[3];
-  double dx;
-  double forceFactor, torqueFactor;
   int nodeF_is_double;
   double* fh;
   double* th;

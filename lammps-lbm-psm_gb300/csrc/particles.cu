@@ -80,11 +80,14 @@ __global__ void img_prep_kernel(MapParams p) {
   if (mine) {
     const Geom& g = p.g;
     im.tag = p.tag[i];
+    im.bidx = p.img_box ? p.img_box[i] : 0;
+    im.zoff = im.bidx * g.bz;
+    const BoxParams& bp = p.box[im.bidx];
     const double r = p.radius[i] / p.dx;
     im.r = r;
     bool valid = true;
     for (int d = 0; d < 3; ++d) {
-      const double xl = local_centre(p.x[3 * i + d], p.origin[d], p.dx);
+      const double xl = local_centre(p.x[3 * i + d], bp.origin[d], p.dx);
       im.xl[d] = xl;
       int lo = (int)(xl - r) - 2;
       int hi = (int)(xl + r) + 2;
@@ -103,11 +106,12 @@ __global__ void img_prep_kernel(MapParams p) {
         slo = lo;
         shi = hi;
       }
-      im.lo[d] = slo;
-      im.hi[d] = shi;
+      const int z0 = d == 2 ? im.zoff : 0;  // boxes of an ensemble stack along z
+      im.lo[d] = slo + z0;
+      im.hi[d] = shi + z0;
       if (slo >= shi) valid = false;
-      im.uT[d] = p.v[3 * i + d] / p.Uc * p.u_lb;
-      im.om[d] = p.omega[3 * i + d] * p.tc * p.dt_d;
+      im.uT[d] = p.v[3 * i + d] / bp.Uc * bp.u_lb;
+      im.om[d] = p.omega[3 * i + d] * bp.tc * bp.dt_d;
       im.uTf[d] = (float)im.uT[d];
       im.omf[d] = (float)im.om[d];
     }
@@ -146,7 +150,7 @@ __global__ void img_prep_kernel(MapParams p) {
       bool solo = true;
       for (int d = 0; d < g.dim; ++d) {
         const int w = ((int)(im.xl[d] + r) + 2) - ((int)(im.xl[d] - r) - 2);
-        if (g.per[d] && w >= g.S[d]) solo = false;
+        if (g.per[d] && w >= (d == 2 ? g.bz : g.S[d])) solo = false;
       }
       im.solo = solo ? 1 : 0;
       for (int d = 0; d < 3; ++d) {
@@ -362,7 +366,7 @@ __global__ void __launch_bounds__(SFC_THREADS) sf_classify_kernel(MapParams p) {
       const int q2 = (int)fast_div((unsigned)q1, fy);
       const int hx = im.lo[0] + li - q1 * wx + g.off[0];
       const int hy = im.lo[1] + q1 - q2 * wy + g.off[1];
-      const int hz = im.lo[2] + q2 + g.off[2];
+      const int hz = im.lo[2] - im.zoff + q2 + g.off[2];  // z in the box's own frame
       float dxf, dyf, dzf;
       const int c = classify_node(hx, hy, hz, im, dxf, dyf, dzf);
       if (c >= 0) {
@@ -660,7 +664,8 @@ __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
   const int sz = blockIdx.z * p.cb[2] + threadIdx.z;
   if (sx >= g.S[0] || sy >= g.S[1] || sz >= g.S[2]) return;
   const long long n = node_index(g, sx, sy, sz);
-  const int hi = sx + g.off[0], hj = sy + g.off[1], hk = sz + g.off[2];
+  const int hi = sx + g.off[0], hj = sy + g.off[1];
+  const int hk = sz - box_of_z(g, sz) * g.bz + g.off[2];  // z in the box's own frame
   const int* lst = p.list + p.cell_off[c];
   int id[2] = {0, 0};
   double eps[2] = {0.0, 0.0};
@@ -780,7 +785,8 @@ __global__ void __launch_bounds__(512) node_apply32_kernel(MapParams p) {
   const int sz = blockIdx.z * p.cb[2] + threadIdx.z;
   if (sx >= g.S[0] || sy >= g.S[1] || sz >= g.S[2]) return;
   const long long n = node_index(g, sx, sy, sz);
-  const int hi = sx + g.off[0], hj = sy + g.off[1], hk = sz + g.off[2];
+  const int hi = sx + g.off[0], hj = sy + g.off[1];
+  const int hk = sz - box_of_z(g, sz) * g.bz + g.off[2];  // z in the box's own frame
   const int* lst = p.list + p.cell_off[c];
   int id[2] = {0, 0};
   float4 rec[2];
@@ -937,7 +943,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
   for (int k = 0; k < 12; ++k) acc[k] = 0.0;
   if (wx > 0 && wy > 0 && wz > 0) {
     const long long total = (long long)wx * wy * wz;
-    const double ff = p.forceFactor, tf = p.torqueFactor;
+    const double ff = p.box[bx.bidx].forceFactor, tf = p.box[bx.bidx].torqueFactor;
     const double* nodeF = static_cast<const double*>(p.tab.nodeF);
     // x fastest: consecutive threads read consecutive nodes
     const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
@@ -948,7 +954,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
       const int j = bx.qlo[1] + q1 - q2 * wy;
       const int k = bx.qlo[2] + q2;
       if (bx.solo && beyond_rP(bx, i, j, k)) continue;
-      const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
+      const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2] + bx.zoff);
       const int2 id = p.tab.ids[n];
       int slot;
       if (tag == id.x)
@@ -1016,7 +1022,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
       const int j = bx.qlo[1] + q1 - q2 * wy;
       const int k = bx.qlo[2] + q2;
       if (bx.solo && beyond_rP(bx, i, j, k)) continue;
-      const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2]);
+      const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2] + bx.zoff);
       const int2 id = p.tab.ids[n];
       int slot;
       if (tag == id.x)
@@ -1084,11 +1090,11 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
     }
     const double sum = (double)sh + (double)sl;
     if (q < 3)
-      p.fh[3 * ip + q] = sum * p.forceFactor;
+      p.fh[3 * ip + q] = sum * p.box[bx.bidx].forceFactor;
     else if (q < 6)
-      p.th[3 * ip + (q - 3)] = sum * p.torqueFactor;
+      p.th[3 * ip + (q - 3)] = sum * p.box[bx.bidx].torqueFactor;
     else
-      p.S[6 * ip + (q - 6)] = -(sum * p.torqueFactor);
+      p.S[6 * ip + (q - 6)] = -(sum * p.box[bx.bidx].torqueFactor);
   }
 }
 

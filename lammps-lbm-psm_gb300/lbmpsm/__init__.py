@@ -38,6 +38,7 @@ SYMBOLS = (
     "lbmpsm_export_fields", "lbmpsm_get_populations", "lbmpsm_set_populations",
     "lbmpsm_get_particle_table", "lbmpsm_check", "lbmpsm_synchronize", "lbmpsm_stream",
     "lbmpsm_run_fixed", "lbmpsm_read_forces", "lbmpsm_export_fields_static",
+    "lbmpsm_create_batch", "lbmpsm_step_batch", "lbmpsm_select_box",
 )
 
 
@@ -113,6 +114,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.lbmpsm_read_forces.argtypes = [H, C.c_int, _D, _D, _D]
     lib.lbmpsm_export_fields_static.argtypes = [H, C.c_int, C.c_double, C.c_double, C.c_double,
                                                 C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.lbmpsm_create_batch.argtypes = [C.c_int, C.POINTER(FixParams), C.POINTER(Options),
+                                        C.POINTER(H)]
+    lib.lbmpsm_step_batch.argtypes = [H, C.c_int, _I, _I, _D, _D, _D, _D, _D, _D, _D]
+    lib.lbmpsm_select_box.argtypes = [H, C.c_int]
     _lib = lib
     return lib
 
@@ -276,3 +281,66 @@ class Lattice:
                 idx[d] = self.local[d] - 1
                 m[tuple(idx)] = False
         return m
+
+
+def _fix_params(dimension=3, boxlo=(0.0, 0.0, 0.0), prd=None, periodic=(1, 1, 1), nevery=1,
+                Nlc=None, lc=None, rho=1.0, nu=None, Re=None, tau=0.7, Fext=(0.0, 0.0, 0.0)):
+    p = FixParams()
+    p.dimension = dimension
+    p.boxlo = (C.c_double * 3)(*boxlo)
+    p.prd = (C.c_double * 3)(*prd)
+    p.periodic = (C.c_int * 3)(*[int(v) for v in periodic])
+    p.nevery, p.Nlc, p.lc, p.rho, p.nu, p.Re, p.tau = nevery, Nlc, lc, rho, nu, Re, tau
+    p.Fext = (C.c_double * 3)(*Fext)
+    return p
+
+
+class Ensemble(Lattice):
+    """Many independent boxes of equal lattice geometry in one device
+    allocation, advanced by one set of kernels per step
+    (lbmpsm_create_batch).  ``boxes`` is a list of keyword dicts with the
+    arguments of :class:`Lattice` that describe one box (tau, Fext, boxlo,
+    rho, nu, Re, ...).  Reference-layout calls (populations, export_fields,
+    particle_table) address the box chosen with :meth:`select_box`."""
+
+    def __init__(self, boxes, *, storage: str = "fp64", device: int = 0, max_images: int = 0,
+                 max_radius: float = 0.0, weighting: str = "reference"):
+        self.lib = load()
+        n = len(boxes)
+        arr = (FixParams * n)(*[_fix_params(**b) for b in boxes])
+        o = Options()
+        o.storage = STORAGE[storage]
+        o.device = device
+        o.max_images = max_images
+        o.max_radius = max_radius
+        o.psm_weighting = WEIGHTING[weighting]
+        h = C.c_void_p()
+        rc = self.lib.lbmpsm_create_batch(n, arr, C.byref(o), C.byref(h))
+        if rc != OK:
+            raise LbmPsmError(rc, self.lib.lbmpsm_last_error(None).decode())
+        self.h = h
+        self.nbox = n
+        self.dimension = boxes[0].get("dimension", 3)
+        self.storage = storage
+        lo = boxes[0].get("boxlo", (0.0, 0.0, 0.0))
+        self.origin = (float(lo[0]), float(lo[1]), float(lo[2]) if self.dimension == 3 else 0.0)
+        self.info = self.get_info()
+        self.local = tuple(self.info.local)
+        self.q = self.info.q
+
+    def select_box(self, b: int):
+        self._check(self.lib.lbmpsm_select_box(self.h, int(b)))
+
+    def step(self, box, tag, x, v, omega, radius):
+        box = np.ascontiguousarray(box, dtype=np.int32)
+        tag = np.ascontiguousarray(tag, dtype=np.int32)
+        n = len(tag)
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(n, 3)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(n, 3)
+        omega = np.ascontiguousarray(omega, dtype=np.float64).reshape(n, 3)
+        radius = np.ascontiguousarray(radius, dtype=np.float64).reshape(n)
+        fh = np.zeros((n, 3)); th = np.zeros((n, 3)); S = np.zeros((n, 6))
+        self._check(self.lib.lbmpsm_step_batch(self.h, n, _p(box, _I), _p(tag, _I), _p(x), _p(v),
+                                               _p(omega), _p(radius), _p(fh), _p(th), _p(S)))
+        return fh, th, S
+
