@@ -412,6 +412,161 @@ def run_reference(args, rank, world):
     }
 
 
+# ---------------------------------------------------------------- ensemble
+ENS_BOXES = 512
+ENS_EDGES = (32, 48, 64, 80, 96)
+ENS_SEED = 20261204
+ENS_LC = 12.0  # lattice units: Nlc = 13, lc = 12 gives dx = 1 in every box
+
+
+def ensemble_spec(nbox=ENS_BOXES, seed=ENS_SEED):
+    """The batched-ensemble workload: per box an edge from ENS_EDGES, tau in
+    U[0.6, 1.0], a body force along x in U[1e-7, 1e-5] (lattice units) and
+    1-40 fixed spheres of diameter U[8, 14] placed by seeded random
+    sequential addition with the periodic minimum image (a box takes as many
+    of its drawn spheres as fit within the try budget)."""
+    rng = np.random.default_rng(seed)
+    spec = []
+    for _ in range(nbox):
+        e = int(rng.choice(ENS_EDGES))
+        tau = float(rng.uniform(0.6, 1.0))
+        fx = float(rng.uniform(1e-7, 1e-5))
+        want = int(rng.integers(1, 41))
+        xs = np.zeros((want, 3))
+        rs = np.zeros(want)
+        k = tries = 0
+        while k < want and tries < 400 * want:
+            tries += 1
+            d = rng.uniform(8.0, 14.0)
+            c = rng.uniform(0.0, e, 3)
+            if k:
+                dl = xs[:k] - c
+                dl -= e * np.round(dl / e)
+                if np.any(np.einsum("ij,ij->i", dl, dl) < (d / 2 + rs[:k]) ** 2):
+                    continue
+            xs[k] = c
+            rs[k] = d / 2
+            k += 1
+        spec.append(dict(edge=e, tau=tau, fx=fx, x=xs[:k].copy(), r=rs[:k].copy()))
+    return spec
+
+
+def ensemble_box_params(e, tau, fx):
+    nu = (tau - 0.5) / 3.0
+    return dict(dimension=3, boxlo=(0.0, 0.0, 0.0), prd=(float(e),) * 3, periodic=(1, 1, 1),
+                Nlc=int(ENS_LC) + 1, lc=ENS_LC, rho=1.0, nu=nu, Re=U_WALL * ENS_LC / nu, tau=tau,
+                Fext=(fx, 0.0, 0.0))
+
+
+def ensemble_images(boxes):
+    """Per-box periodic images, concatenated with the box of each image."""
+    from lbmpsm.host import Domain, ghost_images
+    cols = {k: [] for k in ("box", "tag", "x", "v", "omega", "radius")}
+    nloc = []
+    for b, sb in enumerate(boxes):
+        e = sb["edge"]
+        n = len(sb["r"])
+        dom = Domain(3, (0.0, 0.0, 0.0), (float(e),) * 3, (1, 1, 1))
+        g = ghost_images(dom, 7.0 + 3.0, np.arange(1, n + 1), sb["x"], np.zeros((n, 3)),
+                         np.zeros((n, 3)), sb["r"])
+        cols["box"].append(np.full(len(g.tag), b, np.int32))
+        for k, a in (("tag", g.tag), ("x", g.x), ("v", g.v), ("omega", g.omega), ("radius", g.radius)):
+            cols[k].append(a)
+        nloc.append(n)
+    return {k: np.concatenate(v) for k, v in cols.items()}, nloc
+
+
+def run_ensemble(args):
+    """Aggregate MLUPS of the batched-ensemble workload: one ensemble per
+    edge class, all replayed concurrently (one stream each) as CUDA graphs;
+    then FP32 against FP64 drag on a subset of boxes."""
+    import torch
+
+    import lbmpsm
+
+    spec = ensemble_spec(args.boxes)
+    classes = {}
+    for b, sb in enumerate(spec):
+        classes.setdefault(sb["edge"], []).append(b)
+    K, W = args.steps, args.warmup
+
+    def build(boxes, storage):
+        ens = lbmpsm.Ensemble([ensemble_box_params(sb["edge"], sb["tau"], sb["fx"]) for sb in boxes],
+                              storage=storage)
+        img, nloc = ensemble_images(boxes)
+        ens.step(img["box"], img["tag"], img["x"], img["v"], img["omega"], img["radius"])
+        return ens, img, nloc
+
+    ens = {}
+    nodes = 0
+    for e, ids in sorted(classes.items()):
+        ens[e] = build([spec[b] for b in ids], args.storage)
+        nodes += len(ids) * e ** 3
+    for e in ens:
+        ens[e][0].run_fixed(W)
+    for e in ens:
+        ens[e][0].synchronize()
+    torch.cuda.synchronize()
+    streams = {e: torch.cuda.ExternalStream(ens[e][0].stream) for e in ens}
+    first = next(iter(ens))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e0.record(streams[first])
+    ends = {}
+    with ClockSampler(0) as clk:
+        t_a = time.monotonic()
+        for e in ens:
+            streams[e].wait_event(e0)
+            ens[e][0].run_fixed(K)
+            ends[e] = torch.cuda.Event(enable_timing=True)
+            ends[e].record(streams[e])
+        for e in ens:
+            ends[e].synchronize()
+        clk.mark(t_a, time.monotonic())
+    t = max(e0.elapsed_time(ends[e]) for e in ends) / 1e3
+    per_class = {str(e): {"boxes": len(classes[e]), "nodes": len(classes[e]) * e ** 3}
+                 for e in sorted(classes)}
+    for e in list(ens):
+        ens[e][0].close()
+    del ens
+
+    # accuracy: FP32 (or FP16) against FP64 drag per box on a subset, acc_steps steps
+    acc = None
+    if args.acc_boxes > 0:
+        errs = []
+        for e, ids in sorted(classes.items()):
+            sub = [spec[b] for b in ids[:args.acc_boxes]]
+            drag = {}
+            for storage in (args.storage, "fp64"):
+                en, img, nloc = build(sub, storage)
+                en.run_fixed(args.acc_steps - 2)
+                fh = en.step(img["box"], img["tag"], img["x"], img["v"], img["omega"], img["radius"])[0]
+                en.close()
+                # per box: total x-drag of its local spheres (images are box-major, locals first)
+                out, k = [], 0
+                for bi, n in enumerate(nloc):
+                    m = int(np.sum(img["box"] == bi))
+                    out.append(fh[k:k + n, 0].sum())
+                    k += m
+                drag[storage] = np.array(out)
+            errs.extend(np.abs(drag[args.storage] - drag["fp64"]) / np.abs(drag["fp64"]))
+        errs = np.array(errs)
+        acc = {"boxes": int(len(errs)), "steps": args.acc_steps, "vs": "FP64 GPU path",
+               "drag_rel_err_max": float(errs.max()), "drag_rel_err_median": float(np.median(errs))}
+    return {
+        "metric": "batched ensemble aggregate MLUPS (D3Q19 PSM, 1 GB300)",
+        "value": round(nodes * K / t / 1e6, 1), "unit": "MLUPS", "n_gpus": 1, "steps": K,
+        "warmup": W, "ms_per_step": round(t / K * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.boxes} periodic D3Q19 boxes, edges in {list(ENS_EDGES)}, "
+                               "tau U[0.6,1], Fx U[1e-7,1e-5], 1-40 fixed spheres D U[8,14] "
+                               "(seeded RSA)", "nodes": nodes, "storage": args.storage,
+                   "classes": per_class,
+                   "launch": "one ensemble per edge class, one CUDA graph replay per step each, "
+                             "classes concurrent on separate streams"},
+        "accuracy": acc, "clocks": clk.summary(),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -424,6 +579,11 @@ def main():
     ap.add_argument("--edge", type=int, default=EDGE, help="lattice edge (profiling cases)")
     ap.add_argument("--nspheres", type=int, default=NSPHERES)
     ap.add_argument("--storage", choices=["fp32", "fp16"], default="fp32")
+    ap.add_argument("--workload", choices=["suspension", "ensemble"], default="suspension",
+                    help="suspension: the headline line; ensemble: the batched-box workload")
+    ap.add_argument("--boxes", type=int, default=ENS_BOXES)
+    ap.add_argument("--acc-boxes", type=int, default=8, help="ensemble: boxes per class compared with FP64")
+    ap.add_argument("--acc-steps", type=int, default=2000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -431,7 +591,9 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
-    if args.impl == "reference":
+    if args.workload == "ensemble":
+        out = run_ensemble(args) if rank == 0 else None
+    elif args.impl == "reference":
         out = run_reference(args, rank, world)
     else:
         out = run_ours(args, rank, world)
