@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
   const int sz = row / g.S[1];
   const long long n = node_index(g, sx, sy, sz);
   const Nbr nb = make_nbr(g, sx, sy, sz);
-  const BoxParams& bp = p.box[box_of_z(g, sz)];
+  const BoxParams bp = p.box[box_of_z(g, sz)];  // copied: read once, before any store
   double* __restrict__ F = static_cast<double*>(p.f);
   const long long Np = g.Np;
 

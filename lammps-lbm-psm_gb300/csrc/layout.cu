@@ -140,27 +140,74 @@ cudaError_t launch_set_populations(const Geom& g, void* f, int storage, int afte
 constexpr int CHECK_THREADS = 256;
 constexpr int CHECK_BLOCKS = 1024;
 
-template <class L>
-__global__ void check_partial_kernel(Geom g, const void* f, int storage, int after_odd,
-                                     float scale, double* partial, int* status) {
+// Error-free transformation a + b = s + e (Knuth's TwoSum, no contraction).
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fadd_rn(s, -a);
+  e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb));
+}
+
+// Blocks walk x-rows with 32-bit index arithmetic (64-bit integer division
+// is emulated and slow).  FP64 storage sums the populations in FP64.  FP32 /
+// FP16 storage sums each node's deviations g = f - w in FP32 and adds the
+// node sums into double-float accumulators on the FP32 pipe; the weights add
+// up to exactly 1 per node (mass = nodes + sum g) and to 0 in every momentum
+// component.
+template <class L, bool F64>
+__global__ void __launch_bounds__(CHECK_THREADS) check_partial_kernel(Geom g, const void* f,
+                                                                       int storage, int after_odd,
+                                                                       float scale, double* partial,
+                                                                       int* status) {
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+  unsigned nodes = 0;
   bool bad = false;
-  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N;
-       n += (long long)gridDim.x * blockDim.x) {
-    const int sx = (int)(n % g.P0);
-    const int sy = (int)((n / g.P0) % g.S[1]);
-    const int sz = (int)(n / ((long long)g.P0 * g.S[1]));
-    if (sx >= g.S[0]) continue;  // x padding
-    const Nbr nb = make_nbr(g, sx, sy, sz);
-    for (int q = 0; q < L::Q; ++q) {
-      const long long loc = loc_of<L>(g, nb, n, q, after_odd);
-      const double v = loc >= 0 ? load_pop<int>(f, loc, storage, scale, L::w(q)) : L::w(q);
-      if (!isfinite(v)) bad = true;
-      acc[0] += v;
-      acc[1] += v * L::ex(q);
-      acc[2] += v * L::ey(q);
-      acc[3] += v * L::ez(q);
+  const float inv_scale = 1.0f / scale;
+  const int R = g.S[1] * g.S[2];
+  for (int r = blockIdx.x; r < R; r += gridDim.x) {
+    const int sy = r % g.S[1], sz = r / g.S[1];
+    for (int sx = threadIdx.x; sx < g.S[0]; sx += blockDim.x) {
+      const long long n = node_index(g, sx, sy, sz);
+      const Nbr nb = make_nbr(g, sx, sy, sz);
+      if (F64) {
+        for (int q = 0; q < L::Q; ++q) {
+          const long long loc = loc_of<L>(g, nb, n, q, after_odd);
+          const double v = loc >= 0 ? static_cast<const double*>(f)[loc] : L::w(q);
+          if (!isfinite(v)) bad = true;
+          acc[0] += v;
+          acc[1] += v * L::ex(q);
+          acc[2] += v * L::ey(q);
+          acc[3] += v * L::ez(q);
+        }
+      } else {
+        float ns[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < L::Q; ++q) {
+          const long long loc = loc_of<L>(g, nb, n, q, after_odd);
+          float v = 0.0f;
+          if (loc >= 0)
+            v = storage == 1 ? static_cast<const float*>(f)[loc]
+                             : __half2float(static_cast<const __half*>(f)[loc]) * inv_scale;
+          if (!isfinite(v)) bad = true;
+          ns[0] += v;
+          if (L::ex(q)) ns[1] += L::ex(q) > 0 ? v : -v;
+          if (L::ey(q)) ns[2] += L::ey(q) > 0 ? v : -v;
+          if (L::ez(q)) ns[3] += L::ez(q) > 0 ? v : -v;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float sv, e;
+          two_sum_f(hi[k], ns[k], sv, e);
+          hi[k] = sv;
+          lo[k] = __fadd_rn(lo[k], e);
+        }
+        ++nodes;
+      }
     }
+  }
+  if (!F64) {
+    acc[0] = (double)hi[0] + (double)lo[0] + (double)nodes;
+    for (int k = 1; k < 4; ++k) acc[k] = (double)hi[k] + (double)lo[k];
   }
   if (bad) atomicOr(status, STATUS_NONFINITE);
   for (int k = 0; k < 4; ++k)
@@ -189,12 +236,21 @@ __global__ void check_final_kernel(const double* partial, int nblocks, double* a
 cudaError_t launch_check(const Geom& g, const void* f, int storage, int after_odd, float scale16,
                          double* acc4, int* status, cudaStream_t st) {
   double* partial = acc4 + 4;
-  if (g.dim == 2)
-    check_partial_kernel<D2Q9><<<CHECK_BLOCKS, CHECK_THREADS, 0, st>>>(g, f, storage, after_odd,
-                                                                       scale16, partial, status);
-  else
-    check_partial_kernel<D3Q19><<<CHECK_BLOCKS, CHECK_THREADS, 0, st>>>(g, f, storage, after_odd,
-                                                                        scale16, partial, status);
+  if (g.dim == 2) {
+    if (storage == 0)
+      check_partial_kernel<D2Q9, true><<<CHECK_BLOCKS, CHECK_THREADS, 0, st>>>(
+          g, f, storage, after_odd, scale16, partial, status);
+    else
+      check_partial_kernel<D2Q9, false><<<CHECK_BLOCKS, CHECK_THREADS, 0, st>>>(
+          g, f, storage, after_odd, scale16, partial, status);
+  } else {
+    if (storage == 0)
+      check_partial_kernel<D3Q19, true><<<CHECK_BLOCKS, CHECK_THREADS, 0, st>>>(
+          g, f, storage, after_odd, scale16, partial, status);
+    else
+      check_partial_kernel<D3Q19, false><<<CHECK_BLOCKS, CHECK_THREADS, 0, st>>>(
+          g, f, storage, after_odd, scale16, partial, status);
+  }
   check_final_kernel<<<1, 32, 0, st>>>(partial, CHECK_BLOCKS, acc4);
   return cudaGetLastError();
 }

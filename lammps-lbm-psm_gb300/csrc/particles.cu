@@ -629,11 +629,6 @@ __global__ void __launch_bounds__(SFS_THREADS) sf_shell_kernel(MapParams p) {
   }
 }
 
-// Phase 2 of the map: per node, the images whose boxes contain it, in image
-// order, through the 4-way update of setParticlesOnLattice
-// (src/LBM_PSM_exchangeParticleData.cpp:69-106) on the two-slot table
-// (setParticleOnLattice / setToZero, src/LBM_PSM_lattice.cpp:257-324).
-// The table is written back only where it changed.
 // Phase 2 of the map, per node: the images whose boxes contain it, in image
 // order (the cell list is sorted), through the update of setParticlesOnLattice
 // (src/LBM_PSM_exchangeParticleData.cpp:69-106) on the two-slot table
