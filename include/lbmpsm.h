@@ -238,6 +238,49 @@ int lbmpsm_select_box(lbmpsm_handle* h, int box);
 int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, double B0, double rho0,
                                 double u0, void* solid, void* rho, void* u);
 
+/* Sensitivities of the time-averaged drag (the reference has
+ * no adjoint; the forward step is lbmpsm_step's).  Both calls run nsteps
+ * ordinary coupling steps with one fixed set of particle images -- exactly
+ * the launches of nsteps lbmpsm_step calls with these arrays, so the lattice
+ * ends where those calls leave it -- and differentiate
+ *
+ *   J = 1/M * sum_{t=t0..t1} sum_images  direction . F_image(t),  M = t1-t0+1,
+ *
+ * F_image the hydrodynamic force lbmpsm_step returns at step t (steps
+ * numbered 1..nsteps from the call).  Parameters: tau (the relaxation time,
+ * with the unit factors of lbmpsm_get_info held fixed), Fext (as in
+ * lbmpsm_fix_params) and the image centres.  The solid fraction of a node is
+ * a sub-cell count (calcSolidFraction), piecewise constant in the centre;
+ * its centre derivative is taken as the central difference of that count at
+ * +-centre_step (physical units), the quantity a central finite difference of
+ * J with that step sees to first order.  Ghost images carry their own rows:
+ * sum them into their owner like forces.
+ *
+ * Needs FP64 storage, one box, every axis periodic and no boundary
+ * condition; a node in the surface shells of more than two particles, or of
+ * two images of one particle, is rejected (LBMPSM_ERR_ARG).  Both calls
+ * allocate their scratch on entry and free it on return.
+ *
+ * lbmpsm_adjoint_drag: reverse sweep.  The state before every
+ * checkpoint_every-th step is kept in HBM; the reverse pass recomputes each
+ * segment from its checkpoint.  Device memory: (nsteps/checkpoint_every +
+ * checkpoint_every + 1) population arrays (FP64, Q per node).  Outputs (any
+ * may be NULL except dJ_dx when n > 0): J; dJ/dtau; dJ/dFext[3]; dJ/dx[3n]
+ * per image row; the total drag along direction of every step [nsteps].
+ *
+ * lbmpsm_tangent_drag: forward-mode sweep along (dtau, dFext[3], dx[3n]);
+ * dFext and dx may be NULL (zero).  Outputs J and dJ = grad J . direction. */
+int lbmpsm_adjoint_drag(lbmpsm_handle* h, int n, const int* tag, const double* x,
+                        const double* v, const double* omega, const double* radius, int nsteps,
+                        int t0, int t1, const double* direction, int checkpoint_every,
+                        double centre_step, double* J, double* dJ_dtau, double* dJ_dFext,
+                        double* dJ_dx, double* drag_per_step);
+int lbmpsm_tangent_drag(lbmpsm_handle* h, int n, const int* tag, const double* x,
+                        const double* v, const double* omega, const double* radius, int nsteps,
+                        int t0, int t1, const double* direction, double centre_step,
+                        double dtau, const double* dFext, const double* dx, double* J,
+                        double* dJ);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,8 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I",
           os.path.join(ROOT, "include")]
 # units whose FP64 arithmetic must not be contracted into FMAs
-NO_FMA = {"collide_f64", "particles", "layout", "adjoint"}
-UNITS = ["collide_f64", "collide_lowp", "particles", "layout", "capi"]
+NO_FMA = {"collide_f64", "particles", "layout"}
+UNITS = ["collide_f64", "collide_lowp", "particles", "layout", "adjoint", "capi"]
 
 
 def nvcc() -> str:

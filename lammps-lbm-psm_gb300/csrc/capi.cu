@@ -830,13 +830,10 @@ int lbmpsm_set_bc(lbmpsm_handle* h, int bc_type) {
 }  // extern "C"
 
 namespace {
-// one coupling step with host arrays; box (may be null) gives each image's box
-int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
-              const double* v, const double* omega, const double* radius, double* fh, double* th,
-              double* stresslet) {
-  if (!h || n < 0) return LBMPSM_ERR_ARG;
-  if (n > 0 && (!tag || !x || !v || !omega || !radius || !fh || !th || !stresslet))
-    return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
+// Copy one set of particle images (host arrays) to the handle's device
+// buffers through pinned memory; box (may be null) gives each image's box.
+int stage_images(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
+                 const double* v, const double* omega, const double* radius) {
   if (box) {
     for (int i = 0; i < n; ++i)
       if (box[i] < 0 || box[i] >= h->nbox)
@@ -851,14 +848,13 @@ int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const dou
     return fail(h, LBMPSM_ERR_NUMERIC, "non-finite particle position or radius");
   int rc = ensure_particles(h, n, std::max(rmax, h->opt.max_radius));
   if (rc) return rc;
-  // pinned staging: tags | boxes | x | v | omega | radius | outputs
+  // pinned staging: tags | boxes | x | v | omega | radius | outputs (10*cap doubles after x)
   const size_t cap = (size_t)h->cap;
   char* st = static_cast<char*>(h->h_stage);
   const size_t iblk = (sizeof(int) * cap + 15) & ~(size_t)15;
   int* stag = reinterpret_cast<int*>(st);
   int* sbox = reinterpret_cast<int*>(st + iblk);
   double* sx = reinterpret_cast<double*>(st + 2 * iblk);
-  double* out = sx + 10 * cap;
   if (h->step_boxes != (box != nullptr)) drop_graphs(h);  // the map reads the boxes or not
   h->step_boxes = box != nullptr;
   if (n > 0) {
@@ -877,6 +873,22 @@ int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const dou
     CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw, sx, sizeof(double) * 10 * nn, cudaMemcpyHostToDevice,
                                 h->stream));
   }
+  return LBMPSM_OK;
+}
+
+// one coupling step with host arrays; box (may be null) gives each image's box
+int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
+              const double* v, const double* omega, const double* radius, double* fh, double* th,
+              double* stresslet) {
+  if (!h || n < 0) return LBMPSM_ERR_ARG;
+  if (n > 0 && (!tag || !x || !v || !omega || !radius || !fh || !th || !stresslet))
+    return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
+  int rc = stage_images(h, n, box, tag, x, v, omega, radius);
+  if (rc) return rc;
+  const size_t cap = (size_t)h->cap;
+  char* st = static_cast<char*>(h->h_stage);
+  const size_t iblk = (sizeof(int) * cap + 15) & ~(size_t)15;
+  double* out = reinterpret_cast<double*>(st + 2 * iblk) + 10 * cap;
   rc = enqueue_step(h, n);
   if (rc) return rc;
   if (n > 0) {
@@ -1185,3 +1197,372 @@ extern "C" int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, doub
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return LBMPSM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Adjoint and tangent of the time-averaged drag (lbmpsm_adjoint_drag,
+// lbmpsm_tangent_drag).
+//
+// Both calls run nsteps ordinary coupling steps with one fixed set of
+// particle images -- the same map / collide / reduce launches as nsteps
+// lbmpsm_step calls, so the lattice ends where those calls would leave it and
+// J is the average of the forces they would return -- and differentiate
+//   J = 1/M sum_{t=t0..t1} sum_images d . F_image(t),   M = t1 - t0 + 1,
+// with respect to tau, Fext and the image centres (kernels in adjoint.cu).
+//
+// The adjoint keeps the state before every checkpoint_every-th step in HBM
+// during the forward pass; the reverse pass recomputes each segment's states
+// from its checkpoint (out-of-place FP64 collides into a segment store) and
+// walks the segment backwards.  The tangent runs beside the forward pass.
+namespace {
+
+struct AdjScratch {
+  std::vector<void*> blocks;
+  ~AdjScratch() {
+    for (void* p : blocks) cudaFree(p);
+  }
+  template <typename T>
+  cudaError_t get(T** p, size_t bytes) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e == cudaSuccess) {
+      blocks.push_back(q);
+      *p = static_cast<T*>(q);
+    }
+    return e;
+  }
+};
+
+int adj_validate(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
+                 const double* omega, const double* radius, int nsteps, int t0, int t1,
+                 const double* direction, double centre_step, const char* who) {
+  const std::string w = who;
+  if (h->opt.storage != LBMPSM_STORAGE_FP64)
+    return fail(h, LBMPSM_ERR_STATE, w + ": the adjoint and tangent run on FP64 storage");
+  if (h->nbox > 1) return fail(h, LBMPSM_ERR_STATE, w + ": needs a lattice of one box");
+  if (!h->faces.empty())
+    return fail(h, LBMPSM_ERR_STATE, w + ": needs a lattice without boundary conditions");
+  for (int d = 0; d < h->g.dim; ++d)
+    if (!h->prm.periodic[d])
+      return fail(h, LBMPSM_ERR_STATE, w + ": needs a fully periodic lattice");
+  if (n < 0 || nsteps < 1 || t0 < 1 || t1 < t0 || t1 > nsteps)
+    return fail(h, LBMPSM_ERR_ARG, w + ": needs 1 <= t0 <= t1 <= nsteps and n >= 0");
+  if (n > 0 && (!tag || !x || !v || !omega || !radius))
+    return fail(h, LBMPSM_ERR_ARG, w + ": NULL particle array");
+  if (!direction || !std::isfinite(direction[0]) || !std::isfinite(direction[1]) ||
+      !std::isfinite(direction[2]))
+    return fail(h, LBMPSM_ERR_ARG, w + ": the drag direction must be finite");
+  if (!(centre_step > 0.0) || !std::isfinite(centre_step))
+    return fail(h, LBMPSM_ERR_ARG, w + ": centre_step must be positive");
+  return LBMPSM_OK;
+}
+
+int adj_alloc_nodes(lbmpsm_handle* h, AdjScratch& sc, AdjNodes& an) {
+  const size_t N = (size_t)h->g.N;
+  CUDA_TRY(h, sc.get(&an.band, N));
+  CUDA_TRY(h, sc.get(&an.tag, sizeof(int2) * N));
+  CUDA_TRY(h, sc.get(&an.us, sizeof(double) * 6 * N));
+  CUDA_TRY(h, sc.get(&an.cw, sizeof(int2) * N));
+  CUDA_TRY(h, sc.get(&an.sigma, sizeof(double) * 2 * N));
+  CUDA_TRY(h, sc.get(&an.edot, sizeof(double) * 2 * N));
+  CUDA_TRY(h, cudaMemsetAsync(an.band, 0, N, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(an.tag, 0, sizeof(int2) * N, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(an.us, 0, sizeof(double) * 6 * N, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(an.cw, 0, sizeof(int2) * N, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(an.sigma, 0, sizeof(double) * 2 * N, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(an.edot, 0, sizeof(double) * 2 * N, h->stream));
+  return LBMPSM_OK;
+}
+
+// slot entries and count weights from the table and the cell lists of the map
+// that just ran (n > 0)
+int adj_entries(lbmpsm_handle* h, const AdjNodes& an, int n, double centre_step) {
+  if (n == 0) return LBMPSM_OK;
+  AdjSetup s{};
+  s.g = h->g;
+  s.tab = h->tab;
+  s.an = an;
+  s.img = h->d_img;
+  s.n = n;
+  const int ncells = h->C[0] * h->C[1] * h->C[2];
+  s.cell_count = h->d_cells;
+  s.cell_off = h->d_cells + ncells;
+  s.list = h->d_list;
+  for (int d = 0; d < 3; ++d) {
+    s.cb[d] = h->cb[d];
+    s.C[d] = h->C[d];
+  }
+  s.h0 = h->g.dim == 3 ? std::sqrt(3.1) / 2.0 : std::sqrt(2.1) / 2.0;
+  s.hl = centre_step / h->dx;
+  s.status = h->d_status;
+  CUDA_TRY(h, launch_adj_entries(s, h->stream));
+  return LBMPSM_OK;
+}
+
+AdjParams adj_params(const lbmpsm_handle* h, const AdjNodes& an, double* part,
+                     const double* direction) {
+  AdjParams p{};
+  p.g = h->g;
+  p.tab = h->tab;
+  p.bp = h->boxes[0];
+  p.weighting = h->opt.psm_weighting;
+  p.an = an;
+  p.part = part;
+  for (int d = 0; d < 3; ++d) p.d[d] = direction[d];
+  return p;
+}
+
+AdjCentre adj_centre(const lbmpsm_handle* h, const AdjNodes& an, int n, double centre_step) {
+  AdjCentre c{};
+  c.g = h->g;
+  c.tab = h->tab;
+  c.an = an;
+  c.img = h->d_img;
+  c.n = n;
+  c.x = h->d_xvw;
+  for (int d = 0; d < 3; ++d) c.origin[d] = h->boxes[0].origin[d];
+  c.dx = h->dx;
+  c.h = centre_step;
+  c.h0 = h->g.dim == 3 ? std::sqrt(3.1) / 2.0 : std::sqrt(2.1) / 2.0;
+  c.tau = h->boxes[0].tau;
+  c.weighting = h->opt.psm_weighting;
+  return c;
+}
+
+// one out-of-place FP64 collide (no macro store): dst = step(src) at parity odd
+int collide_into(lbmpsm_handle* h, const double* src, double* dst, int odd) {
+  CollideParams p{};
+  p.g = h->g;
+  p.f = dst;
+  p.fsrc = src;
+  p.tab = h->tab;
+  p.weighting = h->opt.psm_weighting;
+  p.box = h->d_box;
+  p.has_force = h->any_force ? 1 : 0;
+  p.invCs2 = h->invCs2;
+  p.invCs4 = h->invCs4;
+  p.status = h->d_status;
+  CUDA_TRY(h, launch_collide_f64(p, odd, h->stream));
+  return LBMPSM_OK;
+}
+
+int adj_status(lbmpsm_handle* h, const char* who) {
+  int st = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (st & (STATUS_ADJ_CROWDED | STATUS_ADJ_SAME_TAG)) {
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return fail(h, LBMPSM_ERR_ARG,
+                std::string(who) +
+                    ((st & STATUS_ADJ_CROWDED)
+                         ? ": a node lies in the surface shells of more than two particles"
+                         : ": two images of one particle share a surface node"));
+  }
+  return read_status(h);
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbmpsm_adjoint_drag(lbmpsm_handle* h, int n, const int* tag, const double* x,
+                        const double* v, const double* omega, const double* radius, int nsteps,
+                        int t0, int t1, const double* direction, int checkpoint_every,
+                        double centre_step, double* J, double* dJ_dtau, double* dJ_dFext,
+                        double* dJ_dx, double* drag_per_step) {
+  if (!h) return LBMPSM_ERR_ARG;
+  const char* who = "lbmpsm_adjoint_drag";
+  int rc = adj_validate(h, n, tag, x, v, omega, radius, nsteps, t0, t1, direction, centre_step, who);
+  if (rc) return rc;
+  if (checkpoint_every < 1) return fail(h, LBMPSM_ERR_ARG, std::string(who) + ": checkpoint_every must be >= 1");
+  if (n > 0 && !dJ_dx) return fail(h, LBMPSM_ERR_ARG, std::string(who) + ": dJ_dx is NULL");
+  rc = stage_images(h, n, nullptr, tag, x, v, omega, radius);
+  if (rc) return rc;
+  const int T = nsteps, K = std::min(checkpoint_every, nsteps);
+  const int nseg = (T + K - 1) / K;
+  const size_t state = sizeof(double) * (size_t)h->g.Np * h->g.Q;
+  const size_t nstates = (size_t)nseg + (size_t)(K - 1) + 2;
+  {
+    size_t fr = 0, tot = 0;
+    CUDA_TRY(h, cudaMemGetInfo(&fr, &tot));
+    const size_t need = nstates * state + (size_t)h->g.N * 88;
+    if (need + (size_t)(256u << 20) > fr)
+      return fail(h, LBMPSM_ERR_NOMEM,
+                  std::string(who) + ": checkpoints and the segment store need " +
+                      std::to_string(need) + " bytes of device memory, " + std::to_string(fr) +
+                      " are free; choose checkpoint_every near sqrt(nsteps)");
+  }
+  AdjScratch sc;
+  AdjNodes an{};
+  rc = adj_alloc_nodes(h, sc, an);
+  if (rc) return rc;
+  const long long nb = adj_blocks(h->g);
+  double *part = nullptr, *sums = nullptr, *drag = nullptr, *gx = nullptr;
+  CUDA_TRY(h, sc.get(&part, sizeof(double) * ADJ_PART * (size_t)nb));
+  CUDA_TRY(h, sc.get(&sums, sizeof(double) * ADJ_PART));
+  CUDA_TRY(h, sc.get(&drag, sizeof(double) * (size_t)T));
+  CUDA_TRY(h, sc.get(&gx, sizeof(double) * 3 * (size_t)std::max(n, 1)));
+  CUDA_TRY(h, cudaMemsetAsync(part, 0, sizeof(double) * ADJ_PART * (size_t)nb, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(drag, 0, sizeof(double) * (size_t)T, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(gx, 0, sizeof(double) * 3 * (size_t)std::max(n, 1), h->stream));
+  std::vector<double*> ckpt((size_t)nseg), store((size_t)std::max(K - 1, 0));
+  for (auto& c : ckpt) CUDA_TRY(h, sc.get(&c, state));
+  for (auto& c : store) CUDA_TRY(h, sc.get(&c, state));
+  double* lam[2];
+  for (auto& l : lam) CUDA_TRY(h, sc.get(&l, state));
+  CUDA_TRY(h, cudaMemsetAsync(lam[0], 0, state, h->stream));
+
+  // forward pass: the ordinary steps, a checkpoint before every K-th
+  const long long ts = h->t;
+  for (int t = 1; t <= T; ++t) {
+    if ((t - 1) % K == 0)
+      CUDA_TRY(h, cudaMemcpyAsync(ckpt[(size_t)((t - 1) / K)], h->f, state,
+                                  cudaMemcpyDeviceToDevice, h->stream));
+    rc = enqueue_step(h, n);
+    if (rc) return rc;
+    if (t == 1) {
+      rc = adj_entries(h, an, n, centre_step);
+      if (rc) return rc;
+    }
+    if (n > 0)
+      CUDA_TRY(h, launch_adj_drag(h->d_out, n, direction[0], direction[1], direction[2],
+                                  drag + (t - 1), h->stream));
+  }
+  rc = adj_status(h, who);
+  if (rc) return rc;
+
+  // reverse pass, segment by segment
+  const double cwin = h->forceFactor / (double)(t1 - t0 + 1);
+  AdjParams p = adj_params(h, an, part, direction);
+  int cur = 0;  // lam[cur] holds lambda of the step after the one being reversed
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int a = seg * K + 1, b = std::min(a + K - 1, T);
+    auto st_of = [&](int t) { return t == a ? ckpt[(size_t)seg] : store[(size_t)(t - a - 1)]; };
+    for (int t = a + 1; t <= b; ++t) {
+      rc = collide_into(h, st_of(t - 1), st_of(t), (int)((ts + t - 2) & 1));
+      if (rc) return rc;
+    }
+    for (int t = b; t >= a; --t) {
+      p.state = st_of(t);
+      p.odd = (int)((ts + t - 1) & 1);
+      p.lin = lam[cur];
+      p.lout = lam[cur ^ 1];
+      p.c = (t >= t0 && t <= t1) ? cwin : 0.0;
+      CUDA_TRY(h, launch_adj_step(p, 0, h->stream));
+      cur ^= 1;
+    }
+  }
+  AdjCentre c = adj_centre(h, an, n, centre_step);
+  c.out = gx;
+  CUDA_TRY(h, launch_adj_centre(c, h->stream));
+  CUDA_TRY(h, launch_adj_sum(part, nb, sums, h->stream));
+  std::vector<double> hd((size_t)T), hs(ADJ_PART), hx(3 * (size_t)std::max(n, 1));
+  CUDA_TRY(h, cudaMemcpyAsync(hd.data(), drag, sizeof(double) * (size_t)T, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(hs.data(), sums, sizeof(double) * ADJ_PART, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(hx.data(), gx, sizeof(double) * hx.size(), cudaMemcpyDeviceToHost, h->stream));
+  rc = adj_status(h, who);  // synchronises
+  if (rc) return rc;
+  double sJ = 0.0;
+  for (int t = t0; t <= t1; ++t) sJ += hd[(size_t)(t - 1)];
+  const double omega_lb = h->boxes[0].omega;
+  if (J) *J = sJ / (double)(t1 - t0 + 1);
+  if (dJ_dtau) *dJ_dtau = -omega_lb * omega_lb * hs[0] + hs[1];
+  if (dJ_dFext)
+    for (int d = 0; d < 3; ++d) dJ_dFext[d] = hs[2 + d] / h->volumeForceFactor;
+  if (n > 0) std::memcpy(dJ_dx, hx.data(), sizeof(double) * 3 * (size_t)n);
+  if (drag_per_step) std::memcpy(drag_per_step, hd.data(), sizeof(double) * (size_t)T);
+  return LBMPSM_OK;
+}
+
+int lbmpsm_tangent_drag(lbmpsm_handle* h, int n, const int* tag, const double* x,
+                        const double* v, const double* omega, const double* radius, int nsteps,
+                        int t0, int t1, const double* direction, double centre_step,
+                        double dtau, const double* dFext, const double* dx, double* J,
+                        double* dJ) {
+  if (!h) return LBMPSM_ERR_ARG;
+  const char* who = "lbmpsm_tangent_drag";
+  int rc = adj_validate(h, n, tag, x, v, omega, radius, nsteps, t0, t1, direction, centre_step, who);
+  if (rc) return rc;
+  if (!std::isfinite(dtau) || (dFext && !finite_all(dFext, 3)) ||
+      (dx && n > 0 && !finite_all(dx, 3 * (size_t)n)))
+    return fail(h, LBMPSM_ERR_ARG, std::string(who) + ": the direction must be finite");
+  rc = stage_images(h, n, nullptr, tag, x, v, omega, radius);
+  if (rc) return rc;
+  const int T = nsteps;
+  const size_t state = sizeof(double) * (size_t)h->g.Np * h->g.Q;
+  AdjScratch sc;
+  AdjNodes an{};
+  rc = adj_alloc_nodes(h, sc, an);
+  if (rc) return rc;
+  const long long nb = adj_blocks(h->g);
+  double *part = nullptr, *sums = nullptr, *drag = nullptr, *xdot = nullptr, *s1 = nullptr;
+  double* tng[2];
+  CUDA_TRY(h, sc.get(&part, sizeof(double) * ADJ_PART * (size_t)nb));
+  CUDA_TRY(h, sc.get(&sums, sizeof(double) * ADJ_PART));
+  CUDA_TRY(h, sc.get(&drag, sizeof(double) * (size_t)T));
+  CUDA_TRY(h, sc.get(&xdot, sizeof(double) * 3 * (size_t)std::max(n, 1)));
+  CUDA_TRY(h, sc.get(&s1, state));
+  for (auto& t : tng) CUDA_TRY(h, sc.get(&t, state));
+  CUDA_TRY(h, cudaMemsetAsync(part, 0, sizeof(double) * ADJ_PART * (size_t)nb, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(drag, 0, sizeof(double) * (size_t)T, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(tng[0], 0, state, h->stream));
+  std::vector<double> hxd(3 * (size_t)std::max(n, 1), 0.0);
+  if (dx && n > 0) std::memcpy(hxd.data(), dx, sizeof(double) * 3 * (size_t)n);
+  CUDA_TRY(h, cudaMemcpyAsync(xdot, hxd.data(), sizeof(double) * hxd.size(), cudaMemcpyHostToDevice,
+                              h->stream));
+
+  AdjParams p = adj_params(h, an, part, direction);
+  const double omega_lb = h->boxes[0].omega;
+  p.dtau = dtau;
+  p.domega = -omega_lb * omega_lb * dtau;
+  for (int d = 0; d < 3; ++d) p.dF[d] = dFext ? dFext[d] / h->volumeForceFactor : 0.0;
+  const double cwin = h->forceFactor / (double)(t1 - t0 + 1);
+  const long long ts = h->t;
+  int cur = 0;
+  for (int t = 1; t <= T; ++t) {
+    // the tangent step reads the state before this step's collide; the table
+    // it needs exists after the first map, so step 1 runs from a copy
+    if (t == 1) CUDA_TRY(h, cudaMemcpyAsync(s1, h->f, state, cudaMemcpyDeviceToDevice, h->stream));
+    if (t > 1) {
+      p.state = static_cast<const double*>(h->f);
+      p.odd = (int)((ts + t - 1) & 1);
+      p.lin = tng[cur];
+      p.lout = tng[cur ^ 1];
+      p.c = (t >= t0 && t <= t1) ? cwin : 0.0;
+      CUDA_TRY(h, launch_adj_step(p, 1, h->stream));
+      cur ^= 1;
+    }
+    rc = enqueue_step(h, n);
+    if (rc) return rc;
+    if (t == 1) {
+      rc = adj_entries(h, an, n, centre_step);
+      if (rc) return rc;
+      AdjCentre c = adj_centre(h, an, n, centre_step);
+      c.xdot = xdot;
+      CUDA_TRY(h, launch_adj_centre(c, h->stream));
+      p.state = s1;
+      p.odd = (int)(ts & 1);
+      p.lin = tng[cur];
+      p.lout = tng[cur ^ 1];
+      p.c = (t >= t0 && t <= t1) ? cwin : 0.0;
+      CUDA_TRY(h, launch_adj_step(p, 1, h->stream));
+      cur ^= 1;
+    }
+    if (n > 0)
+      CUDA_TRY(h, launch_adj_drag(h->d_out, n, direction[0], direction[1], direction[2],
+                                  drag + (t - 1), h->stream));
+  }
+  CUDA_TRY(h, launch_adj_sum(part, nb, sums, h->stream));
+  std::vector<double> hd((size_t)T), hs(ADJ_PART);
+  CUDA_TRY(h, cudaMemcpyAsync(hd.data(), drag, sizeof(double) * (size_t)T, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(hs.data(), sums, sizeof(double) * ADJ_PART, cudaMemcpyDeviceToHost, h->stream));
+  rc = adj_status(h, who);
+  if (rc) return rc;
+  double sJ = 0.0;
+  for (int t = t0; t <= t1; ++t) sJ += hd[(size_t)(t - 1)];
+  if (J) *J = sJ / (double)(t1 - t0 + 1);
+  if (dJ) *dJ = hs[0];
+  return LBMPSM_OK;
+}
+
+}  // extern "C"

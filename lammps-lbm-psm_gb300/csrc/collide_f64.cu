@@ -137,7 +137,9 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
   const long long n = node_index(g, sx, sy, sz);
   const Nbr nb = make_nbr(g, sx, sy, sz);
   const BoxParams bp = p.box[box_of_z(g, sz)];  // copied: read once, before any store
-  double* __restrict__ F = static_cast<double*>(p.f);
+  double* F = static_cast<double*>(p.f);
+  // in place unless a separate source is given (recomputation of stored states)
+  const double* Fin = p.fsrc ? static_cast<const double*>(p.fsrc) : F;
   const long long Np = g.Np;
 
   double f[Q];
@@ -147,10 +149,10 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
     // incoming population q comes from the node at -e_q
     const bool ok = nbr_ok(nb, -cx, -cy, -cz);
     if (!ODD) {
-      f[q] = ok ? F[q * Np + n] : L::w(q);
+      f[q] = ok ? Fin[q * Np + n] : L::w(q);
     } else {
       const int o = nbr_off(nb, -cx, -cy, -cz);
-      f[q] = ok ? F[L::opp(q) * Np + n + o] : L::w(q);
+      f[q] = ok ? Fin[L::opp(q) * Np + n + o] : L::w(q);
     }
   }
 

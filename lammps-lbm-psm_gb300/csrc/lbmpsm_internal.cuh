@@ -221,6 +221,7 @@ struct CollideParams {
   float scale16;          // FP16 storage: stored value = deviation * scale16
   int* status;            // error word (STATUS_*)
   PipeConfig pipe;
+  const void* fsrc;       // FP64 only: read the populations here and write f (null: in place)
 };
 
 
@@ -324,7 +325,70 @@ struct ReduceParams {
 };
 
 // status bits
-enum : int { STATUS_LIST_OVERFLOW = 1, STATUS_NONFINITE = 2, STATUS_TIMEOUT = 4 };
+enum : int { STATUS_LIST_OVERFLOW = 1, STATUS_NONFINITE = 2, STATUS_TIMEOUT = 4,
+             STATUS_ADJ_CROWDED = 8, STATUS_ADJ_SAME_TAG = 16 };
+
+// ---------------------------------------------------------------- adjoint
+// Dense per-node data of the adjoint and tangent sweeps (N entries each).
+// An "entry" is a table slot: the table's particle when the slot is taken,
+// else the particle that would take it if its solid fraction rose above
+// zero (one whose surface shell holds the node).
+struct AdjNodes {
+  uint8_t* band;   // node in the surface shell of some particle image
+  int2* tag;       // entry tag per slot (0: none)
+  double* us;      // 6N, slot-major: solid velocity of entering particles
+  int2* cw;        // images of the entry's tag whose reduction box holds the node
+  double* sigma;   // 2N: sum over steps of dJ/dB per slot (band nodes)
+  double* edot;    // 2N: tangent solid-fraction rate per slot
+};
+
+struct AdjParams {
+  Geom g;
+  Table tab;
+  BoxParams bp;
+  int weighting;
+  AdjNodes an;
+  const double* state;  // A-A populations before the step (FP64)
+  int odd;              // A-A parity of that state
+  const double* lin;    // adjoint: lambda of the next step; tangent: this step's tangent
+  double* lout;         // adjoint: lambda of this step; tangent: the next step's tangent
+  double c;             // objective weight of this step
+  double d[3];          // drag direction
+  double* part;         // per-block partial sums, ADJ_PART per block
+  double domega, dtau, dF[3];  // tangent direction (lattice units)
+};
+constexpr int ADJ_PART = 5;  // d/domega, d/dtau through B, d/dF[3] (tangent: dJ in [0])
+
+struct AdjSetup {
+  Geom g;
+  Table tab;
+  AdjNodes an;
+  const Img* img;
+  int n;
+  const int* cell_off;
+  const int* cell_count;
+  const int* list;
+  int cb[3], C[3];
+  double h0;    // early-out half-diagonal of calcSolidFraction
+  double hl;    // centre step, lattice units
+  int* status;
+};
+
+struct AdjCentre {
+  Geom g;
+  Table tab;
+  AdjNodes an;
+  const Img* img;
+  int n;
+  const double* x;      // physical image centres (3n)
+  double origin[3], dx;
+  double h;             // centre step, physical units
+  double h0;
+  double tau;
+  int weighting;
+  const double* xdot;   // tangent: centre direction per image (3n); null for the adjoint
+  double* out;          // adjoint: dJ/dx per image (3n)
+};
 
 // ---------------------------------------------------------------- launchers
 // collide.cu / collide_f32.cu
@@ -356,5 +420,13 @@ cudaError_t launch_export_fields(const Geom& g, const Table& t, const double* rh
                                  const double* u, int as_double, double B0, double rho0,
                                  double u0, void* solid_out, void* rho_out, void* u_out,
                                  cudaStream_t st);
+// adjoint.cu
+long long adj_blocks(const Geom& g);
+cudaError_t launch_adj_entries(const AdjSetup& s, cudaStream_t st);
+cudaError_t launch_adj_step(const AdjParams& p, int tangent, cudaStream_t st);
+cudaError_t launch_adj_centre(const AdjCentre& c, cudaStream_t st);
+cudaError_t launch_adj_drag(const double* fh, int n, double d0, double d1, double d2,
+                            double* out, cudaStream_t st);
+cudaError_t launch_adj_sum(const double* part, long long nblocks, double* out, cudaStream_t st);
 
 }  // namespace lbmpsm

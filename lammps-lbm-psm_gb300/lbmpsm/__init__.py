@@ -39,6 +39,7 @@ SYMBOLS = (
     "lbmpsm_get_particle_table", "lbmpsm_check", "lbmpsm_synchronize", "lbmpsm_stream",
     "lbmpsm_run_fixed", "lbmpsm_read_forces", "lbmpsm_export_fields_static",
     "lbmpsm_create_batch", "lbmpsm_step_batch", "lbmpsm_select_box",
+    "lbmpsm_adjoint_drag", "lbmpsm_tangent_drag",
 )
 
 
@@ -118,6 +119,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
                                         C.POINTER(H)]
     lib.lbmpsm_step_batch.argtypes = [H, C.c_int, _I, _I, _D, _D, _D, _D, _D, _D, _D]
     lib.lbmpsm_select_box.argtypes = [H, C.c_int]
+    lib.lbmpsm_adjoint_drag.argtypes = [H, C.c_int, _I, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int,
+                                        _D, C.c_int, C.c_double, _D, _D, _D, _D, _D]
+    lib.lbmpsm_tangent_drag.argtypes = [H, C.c_int, _I, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int,
+                                        _D, C.c_double, C.c_double, _D, _D, _D, _D]
     _lib = lib
     return lib
 
@@ -208,6 +213,47 @@ class Lattice:
         self._check(self.lib.lbmpsm_step(self.h, n, _p(tag, _I), _p(x), _p(v), _p(omega),
                                          _p(radius), _p(fh), _p(th), _p(S)))
         return fh, th, S
+
+    @staticmethod
+    def _images(tag, x, v, omega, radius):
+        tag = np.ascontiguousarray(tag, dtype=np.int32)
+        n = len(tag)
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(n, 3)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(n, 3)
+        omega = np.ascontiguousarray(omega, dtype=np.float64).reshape(n, 3)
+        radius = np.ascontiguousarray(radius, dtype=np.float64).reshape(n)
+        return n, tag, x, v, omega, radius
+
+    def adjoint_drag(self, tag, x, v, omega, radius, nsteps, t0, t1, direction=(1.0, 0.0, 0.0),
+                     checkpoint_every=100, centre_step=None):
+        """Run nsteps coupling steps with these images held in place and
+        return J (the drag along ``direction`` averaged over steps t0..t1) with
+        its gradient: dict(J, dtau, dFext[3], dx[n,3] per image row, drag[nsteps])."""
+        n, tag, x, v, omega, radius = self._images(tag, x, v, omega, radius)
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        h = 1e-4 * self.info.dx if centre_step is None else float(centre_step)
+        J = C.c_double(); dtau = C.c_double(); dF = np.zeros(3); dx = np.zeros((max(n, 1), 3))
+        drag = np.zeros(int(nsteps))
+        self._check(self.lib.lbmpsm_adjoint_drag(
+            self.h, n, _p(tag, _I), _p(x), _p(v), _p(omega), _p(radius), int(nsteps), int(t0),
+            int(t1), _p(d), int(checkpoint_every), h, C.byref(J), C.byref(dtau), _p(dF), _p(dx),
+            _p(drag)))
+        return dict(J=J.value, dtau=dtau.value, dFext=dF, dx=dx[:n], drag=drag)
+
+    def tangent_drag(self, tag, x, v, omega, radius, nsteps, t0, t1, direction=(1.0, 0.0, 0.0),
+                     dtau=0.0, dFext=None, dx=None, centre_step=None):
+        """Forward-mode run along (dtau, dFext, dx): returns (J, dJ)."""
+        n, tag, x, v, omega, radius = self._images(tag, x, v, omega, radius)
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        h = 1e-4 * self.info.dx if centre_step is None else float(centre_step)
+        dF = None if dFext is None else np.ascontiguousarray(dFext, dtype=np.float64).reshape(3)
+        dxa = None if dx is None else np.ascontiguousarray(dx, dtype=np.float64).reshape(n, 3)
+        J = C.c_double(); dJ = C.c_double()
+        self._check(self.lib.lbmpsm_tangent_drag(
+            self.h, n, _p(tag, _I), _p(x), _p(v), _p(omega), _p(radius), int(nsteps), int(t0),
+            int(t1), _p(d), h, float(dtau), None if dF is None else _p(dF),
+            None if dxa is None else _p(dxa), C.byref(J), C.byref(dJ)))
+        return J.value, dJ.value
 
     def step_device(self, n, tag_ptr, x_ptr, v_ptr, omega_ptr, radius_ptr, fh_ptr=None,
                     th_ptr=None, s_ptr=None):
