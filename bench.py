@@ -567,6 +567,123 @@ def run_ensemble(args):
     }
 
 
+ADJ_EDGE, ADJ_N, ADJ_D, ADJ_TAU, ADJ_FX, ADJ_SEED = 96, 8, 12.0, 0.7, 1e-6, 2024
+ADJ_T, ADJ_K = 2000, 100
+
+
+def adjoint_params(tau=ADJ_TAU, fx=ADJ_FX, edge=ADJ_EDGE):
+    nu = (tau - 0.5) / 3.0
+    return dict(dimension=3, boxlo=(0.0, 0.0, 0.0), prd=(float(edge),) * 3, periodic=(1, 1, 1),
+                nevery=1, Nlc=int(ADJ_D) + 1, lc=ADJ_D, rho=1.0, nu=nu, Re=0.01 * ADJ_D / nu,
+                tau=tau, Fext=(fx, 0.0, 0.0))
+
+
+def adjoint_images(x=None, edge=ADJ_EDGE):
+    """8 fixed spheres of diameter 12 by seeded random sequential addition
+    (minimum image, gap >= 2 lattice units) and their periodic ghost images."""
+    from lbmpsm.host import Domain, ghost_images
+    r = ADJ_D / 2
+    if x is None:
+        rng = np.random.default_rng(ADJ_SEED)
+        x = np.zeros((ADJ_N, 3))
+        k = 0
+        while k < ADJ_N:
+            c = rng.uniform(0.0, edge, 3)
+            dlt = x[:k] - c
+            dlt -= edge * np.round(dlt / edge)
+            if k and np.min(np.einsum("ij,ij->i", dlt, dlt)) < (2 * r + 2.0) ** 2:
+                continue
+            x[k] = c
+            k += 1
+    dom = Domain(3, (0.0, 0.0, 0.0), (float(edge),) * 3, (1, 1, 1))
+    n = len(x)
+    return ghost_images(dom, r + 3.0, np.arange(1, n + 1), x, np.zeros((n, 3)), np.zeros((n, 3)),
+                        np.full(n, r)), x
+
+
+def adjoint_J(img, T, t0, **kw):
+    """J through the plain step API: steps before the window as one graph
+    replay, the window step by step with the forces read back."""
+    import lbmpsm
+    lat = lbmpsm.Lattice(**adjoint_params(**kw), storage="fp64")
+    a = (img.tag, img.x, img.v, img.omega, img.radius)
+    lat.step(*a)
+    lat.run_fixed(t0 - 2)
+    J = 0.0
+    for _ in range(t0, T + 1):
+        J += float(lat.step(*a)[0][:, 0].sum())
+    lat.close()
+    return J / (T - t0 + 1)
+
+
+def run_adjoint(args):
+    """Cost of the adjoint sweep against the forward steps it differentiates,
+    and its gradient against central finite differences."""
+    import torch
+
+    import lbmpsm
+    from lbmpsm.host import reverse_comm
+
+    E, T, K = args.adj_edge, args.adj_steps, args.adj_checkpoint
+    t0 = T // 2
+    img, x = adjoint_images(edge=E)
+    a = (img.tag, img.x, img.v, img.omega, img.radius)
+    prm = adjoint_params(edge=E)
+    # forward: the same FP64 steps replayed as a CUDA graph
+    fwd = lbmpsm.Lattice(**prm, storage="fp64")
+    fwd.step(*a)
+    fwd.synchronize()
+    st = torch.cuda.ExternalStream(fwd.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    fwd.run_fixed(T - 1)
+    e1.record(st)
+    e1.synchronize()
+    t_fwd = e0.elapsed_time(e1) / 1e3 * T / (T - 1)
+    fwd.close()
+    lat = lbmpsm.Lattice(**prm, storage="fp64")
+    with ClockSampler(0) as clk:
+        t_a = time.monotonic()
+        t = time.perf_counter()
+        R = lat.adjoint_drag(*a, T, t0, T, checkpoint_every=K)
+        t_adj = time.perf_counter() - t
+        clk.mark(t_a, time.monotonic())
+    lat.close()
+    grad = reverse_comm(R["dx"], img.owner, img.swap, img.nlocal)[:img.nlocal]
+    adj = {"dtau": R["dtau"], "dFx": float(R["dFext"][0]), "dx0": float(grad[0, 0])}
+    fd, rel = None, None
+    h, hF = 1e-4, 1e-10
+    if not args.no_fd:
+        fd = {}
+        fd["dtau"] = (adjoint_J(img, T, t0, tau=ADJ_TAU + h, edge=E) -
+                      adjoint_J(img, T, t0, tau=ADJ_TAU - h, edge=E)) / (2 * h)
+        fd["dFx"] = (adjoint_J(img, T, t0, fx=ADJ_FX + hF, edge=E) -
+                     adjoint_J(img, T, t0, fx=ADJ_FX - hF, edge=E)) / (2 * hF)
+        xp, xm = x.copy(), x.copy()
+        xp[0, 0] += h
+        xm[0, 0] -= h
+        fd["dx0"] = (adjoint_J(adjoint_images(xp, E)[0], T, t0, edge=E) -
+                     adjoint_J(adjoint_images(xm, E)[0], T, t0, edge=E)) / (2 * h)
+        rel = {k: abs(adj[k] - fd[k]) / abs(fd[k]) for k in fd}
+    nodes = E ** 3
+    return {
+        "metric": "adjoint cost: d(time-averaged drag)/d(tau, Fext, 24 centres) vs forward, 1 GB300",
+        "value": round(t_adj / t_fwd, 3), "unit": "x forward time", "n_gpus": 1, "steps": T,
+        "warmup": 1, "ms_per_step": round(t_adj / T * 1e3, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"D3Q19 {E}^3 periodic, tau 0.7, Fext (1e-6,0,0), 8 fixed spheres "
+                               f"D=12 (seeded RSA), J = x-drag averaged over steps {t0}-{T}, "
+                               f"checkpoints every {K} steps", "nodes": nodes,
+                   "images": int(len(img.tag)), "storage": "fp64"},
+        "forward_s": round(t_fwd, 4), "adjoint_s": round(t_adj, 4),
+        "adjoint_mlups": round(nodes * T / t_adj / 1e6, 1),
+        "J": R["J"], "gradient": adj, "finite_difference": fd, "rel_err_vs_fd": rel,
+        "fd_steps": {"tau": h, "Fext": hF, "centre": h},
+        "clocks": clk.summary(),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -579,11 +696,16 @@ def main():
     ap.add_argument("--edge", type=int, default=EDGE, help="lattice edge (profiling cases)")
     ap.add_argument("--nspheres", type=int, default=NSPHERES)
     ap.add_argument("--storage", choices=["fp32", "fp16"], default="fp32")
-    ap.add_argument("--workload", choices=["suspension", "ensemble"], default="suspension",
-                    help="suspension: the headline line; ensemble: the batched-box workload")
+    ap.add_argument("--workload", choices=["suspension", "ensemble", "adjoint"], default="suspension",
+                    help="suspension: the headline line; ensemble: the batched-box workload; "
+                         "adjoint: the drag-sensitivity sweep")
     ap.add_argument("--boxes", type=int, default=ENS_BOXES)
     ap.add_argument("--acc-boxes", type=int, default=8, help="ensemble: boxes per class compared with FP64")
     ap.add_argument("--acc-steps", type=int, default=2000)
+    ap.add_argument("--adj-edge", type=int, default=ADJ_EDGE, help="adjoint: lattice edge")
+    ap.add_argument("--adj-steps", type=int, default=ADJ_T, help="adjoint: steps (window: 2nd half)")
+    ap.add_argument("--adj-checkpoint", type=int, default=ADJ_K)
+    ap.add_argument("--no-fd", action="store_true", help="adjoint: skip the finite differences")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -593,6 +715,8 @@ def main():
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
     if args.workload == "ensemble":
         out = run_ensemble(args) if rank == 0 else None
+    elif args.workload == "adjoint":
+        out = run_adjoint(args) if rank == 0 else None
     elif args.impl == "reference":
         out = run_reference(args, rank, world)
     else:
