@@ -53,6 +53,7 @@ struct lbmpsm_handle {
   double* d_xvw = nullptr;  // x | v | omega | radius, each cap entries
   double* d_out = nullptr;  // fh | th | S  (12*cap)
   Img* d_img = nullptr;
+  int4* d_arec = nullptr;   // compact image records of the table update (3 per image)
   int* d_cells = nullptr;   // count | off | fill (3*ncells)
   int* d_list = nullptr;
   unsigned short* d_sfcode = nullptr;  // solid-fraction codes of (image, box node) pairs
@@ -232,6 +233,8 @@ void free_particles(lbmpsm_handle* h) {
   dfree(h->d_xvw);
   dfree(h->d_out);
   dfree(h->d_img);
+  dfree(h->d_arec);
+  h->d_arec = nullptr;
   dfree(h->d_img_box);
   h->d_img_box = nullptr;
   dfree(h->d_list);
@@ -280,6 +283,7 @@ int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
     CUDA_TRY(h, dmalloc(h, &h->d_xvw, sizeof(double) * 10 * cap));
     CUDA_TRY(h, dmalloc(h, &h->d_out, sizeof(double) * 12 * cap));
     CUDA_TRY(h, dmalloc(h, &h->d_img, sizeof(Img) * cap));
+    CUDA_TRY(h, dmalloc(h, &h->d_arec, sizeof(int4) * 3 * cap));
     CUDA_TRY(h, dmalloc(h, &h->d_img_box, sizeof(int) * cap));
     h->h_stage_bytes = (2 * sizeof(int) + sizeof(double) * 10 + sizeof(double) * 12) * (size_t)cap + 64;
     CUDA_TRY(h, cudaMallocHost(&h->h_stage, h->h_stage_bytes));
@@ -403,6 +407,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     m.dx = h->dx;
     m.sqrt2half = h->g.dim == 3 ? std::sqrt(3.1) / 2.0 : std::sqrt(2.1) / 2.0;
     m.img = h->d_img;
+    m.arec = h->d_arec;
     for (int d = 0; d < 3; ++d) {
       m.cb[d] = h->cb[d];
       m.C[d] = h->C[d];

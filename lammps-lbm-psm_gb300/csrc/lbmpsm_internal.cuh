@@ -292,6 +292,10 @@ struct MapParams {
   double dx;
   double sqrt2half;   // sqrt(2.1)/2 in 2-D, sqrt(3.1)/2 in 3-D (host libm)
   Img* img;
+  // per image, three int4 for the table update: (lo0 | hi0 << 16, lo1 | hi1 << 16,
+  // lo2 | hi2 << 16, tag), (sf_off low, sf_off high, box0 | box1 << 16, has_spin),
+  // (uTf[0..2] as bits, 0); an image with an empty box has lo = hi = 0
+  int4* arec;
   int cb[3];          // cell edge (nodes) per axis
   int C[3];           // cells per axis
   int* cell_count;

@@ -189,6 +189,17 @@ __global__ void img_prep_kernel(MapParams p) {
   if (mine) {
     im.sf_off = (long long)(base + incl - vol);
     p.img[i] = im;
+    int4 a = make_int4(0, 0, 0, im.tag), b;
+    if (im.valid)
+      a = make_int4(im.lo[0] | (im.hi[0] << 16), im.lo[1] | (im.hi[1] << 16),
+                    im.lo[2] | (im.hi[2] << 16), im.tag);
+    b = make_int4((int)(unsigned)(unsigned long long)im.sf_off,
+                  (int)(unsigned)((unsigned long long)im.sf_off >> 32),
+                  im.box[0] | (im.box[1] << 16), im.has_spin);
+    p.arec[3 * i] = a;
+    p.arec[3 * i + 1] = b;
+    p.arec[3 * i + 2] = make_int4(__float_as_int(im.uTf[0]), __float_as_int(im.uTf[1]),
+                                  __float_as_int(im.uTf[2]), 0);
   }
   // cell counts, one image of the warp at a time
   unsigned long long pairs = 0;
@@ -767,7 +778,88 @@ __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
 // kernel reads (eps, u_s per slot); the same update rules, no FP64.  The
 // records hold the FP32 roundings of the reference's values (for spinning
 // images the node velocity is formed in FP32).
-__global__ void __launch_bounds__(512) node_apply32_kernel(MapParams p) {
+//
+// One node's update state: the tags of its two slots as they stand after
+// the images applied so far.  Slot records are compared with the table and
+// written through when they change, so only the ids live in registers; the
+// ids and the flag are written back at the end if they changed.
+struct Apply32 {
+  int id0, id1;
+  bool ids_dirty;
+
+  __device__ __forceinline__ void init(int2 ids) {
+    id0 = ids.x;
+    id1 = ids.y;
+    ids_dirty = false;
+  }
+
+  // one image with code cd at node n; nv.yzw is the node velocity it sets
+  __device__ __forceinline__ void image(const MapParams& p, long long n, int tag,
+                                        unsigned short cd, float4 nv) {
+    if (cd == 0) {  // setToZero (src/LBM_PSM_lattice.cpp:302-324)
+      const int m = tag == id0 ? 0 : (tag == id1 ? 1 : -1);
+      if (m >= 0) {
+        if (m == 0) id0 = 0; else id1 = 0;
+        ids_dirty = true;
+        p.tab.rec32[2 * n + m] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      return;
+    }
+    // setParticleOnLattice: matching slot, else the first empty one, else drop
+    int slot = -1;
+    if (id0 == tag)
+      slot = 0;
+    else if (id1 == tag)
+      slot = 1;
+    else if (id0 == 0)
+      slot = 0;
+    else if (id1 == 0)
+      slot = 1;
+    if (slot < 0) return;
+    nv.x = cd == SF_ONE ? 1.0f : p.sf_value32[cd];
+    const int cur = slot == 0 ? id0 : id1;
+    // re-setting a slot to the values it already holds changes nothing
+    if (cur == tag) {
+      const float4 r = p.tab.rec32[2 * n + slot];
+      if (__float_as_int(r.x) == __float_as_int(nv.x) &&
+          __float_as_int(r.y) == __float_as_int(nv.y) &&
+          __float_as_int(r.z) == __float_as_int(nv.z) &&
+          __float_as_int(r.w) == __float_as_int(nv.w))
+        return;
+    } else {
+      if (slot == 0) id0 = tag; else id1 = tag;
+      ids_dirty = true;
+    }
+    p.tab.rec32[2 * n + slot] = nv;
+  }
+
+  __device__ __forceinline__ void store(const MapParams& p, long long n) const {
+    if (ids_dirty) {
+      p.tab.ids[n] = make_int2(id0, id1);
+      p.tab.flag[n] = (uint8_t)((id0 > 0 ? 1 : 0) | (id1 > 0 ? 2 : 0));
+    }
+  }
+};
+
+// rigid-body velocity of node (hi, hj, hk) of a spinning image, in FP32
+// (src/LBM_PSM_exchangeParticleData.cpp:83-89)
+static __device__ __forceinline__ float4 spin_velocity(const Img& im, int hi, int hj, int hk) {
+  const float dx = small_int_to_float(hi - im.xi[0]) - im.xf[0];
+  const float dy = small_int_to_float(hj - im.xi[1]) - im.xf[1];
+  const float dz = small_int_to_float(hk - im.xi[2]) - im.xf[2];
+  return make_float4(0.f, im.uTf[0] + im.omf[1] * dz - im.omf[2] * dy,
+                     im.uTf[1] + im.omf[2] * dx - im.omf[0] * dz,
+                     im.uTf[2] + im.omf[0] * dy - im.omf[1] * dx);
+}
+
+// NPT nodes per thread (z, z + blockDim.z, ... within the cell; one node in
+// 2-D) of a cell that some image box touches.  The images of the cell's list
+// are visited in image order through their compact records (three 16-byte
+// loads instead of the scattered fields of Img), each record serving all the
+// thread's nodes, whose code, slot id and slot record loads are independent;
+// the slot ids are loaded on first use only.
+template <int NPT>
+__global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p) {
   const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
   const int cnt = p.cell_count[c];
   if (cnt == 0) return;
@@ -777,93 +869,74 @@ __global__ void __launch_bounds__(512) node_apply32_kernel(MapParams p) {
   const Geom& g = p.g;
   const int sx = blockIdx.x * p.cb[0] + threadIdx.x;
   const int sy = blockIdx.y * p.cb[1] + threadIdx.y;
-  const int sz = blockIdx.z * p.cb[2] + threadIdx.z;
-  if (sx >= g.S[0] || sy >= g.S[1] || sz >= g.S[2]) return;
-  const long long n = node_index(g, sx, sy, sz);
-  const int hi = sx + g.off[0], hj = sy + g.off[1];
-  const int hk = sz - box_of_z(g, sz) * g.bz + g.off[2];  // z in the box's own frame
+  const int sz0 = blockIdx.z * p.cb[2] + threadIdx.z;
+  if (sx >= g.S[0] || sy >= g.S[1] || sz0 >= g.S[2]) return;
+  const int dz = (int)blockDim.z;
+  const long long n0 = node_index(g, sx, sy, sz0);
+  const long long zstride = (long long)dz * g.P0 * g.S[1];
+  bool has[NPT];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k)
+    has[k] = (int)threadIdx.z + k * dz < p.cb[2] && sz0 + k * dz < g.S[2];
   const int* lst = p.list + p.cell_off[c];
-  int id[2] = {0, 0};
-  float4 rec[2];
-  bool have_ids = false, ids_dirty = false;
-  bool have_rec[2] = {false, false}, slot_dirty[2] = {false, false};
+  Apply32 st[NPT];
+  bool have[NPT];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) have[k] = false;
   for (int t = 0; t < cnt; ++t) {
-    const Img& im = p.img[lst[t]];
-    if (sx < im.lo[0] || sx >= im.hi[0] || sy < im.lo[1] || sy >= im.hi[1] || sz < im.lo[2] ||
-        sz >= im.hi[2])
-      continue;
-    const int li = ((sz - im.lo[2]) * im.box[1] + (sy - im.lo[1])) * im.box[0] + (sx - im.lo[0]);
-    const unsigned short cd = p.sfcode[im.sf_off + li];
-    const int tag = im.tag;
-    if (!have_ids) {
-      const int2 v = p.tab.ids[n];
-      id[0] = v.x;
-      id[1] = v.y;
-      have_ids = true;
+    const int ii = lst[t];
+    const int4 A = p.arec[3 * ii];
+    const unsigned ax = (unsigned)A.x, ay = (unsigned)A.y, az = (unsigned)A.z;
+    const int lo0 = (int)(ax & 0xFFFFu), lo1 = (int)(ay & 0xFFFFu), lo2 = (int)(az & 0xFFFFu);
+    const int hi2 = (int)(az >> 16);
+    if (sx < lo0 || sx >= (int)(ax >> 16) || sy < lo1 || sy >= (int)(ay >> 16)) continue;
+    bool in[NPT];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+      const int z = sz0 + k * dz;
+      in[k] = has[k] && z >= lo2 && z < hi2;
+      any = any || in[k];
     }
-    const int match = tag == id[0] ? 0 : (tag == id[1] ? 1 : -1);
-    if (cd == 0) {  // setToZero (src/LBM_PSM_lattice.cpp:302-324)
-      if (match >= 0) {
-        id[match] = 0;
-        rec[match] = make_float4(0.f, 0.f, 0.f, 0.f);
-        have_rec[match] = true;
-        ids_dirty = true;
-        slot_dirty[match] = true;
+    if (!any) continue;
+    const int4 B = p.arec[3 * ii + 1];
+    const unsigned bz = (unsigned)B.z;
+    const int bx = (int)(bz & 0xFFFFu), by = (int)(bz >> 16);
+    const long long off = (long long)(((unsigned long long)(unsigned)B.y << 32) |
+                                      (unsigned long long)(unsigned)B.x) +
+                          (long long)(sy - lo1) * bx + (sx - lo0);
+    const long long plane = (long long)by * bx;
+    unsigned short cd[NPT];
+#pragma unroll
+    for (int k = 0; k < NPT; ++k)
+      cd[k] = in[k] ? p.sfcode[off + (sz0 + k * dz - lo2) * plane] : (unsigned short)0;
+#pragma unroll
+    for (int k = 0; k < NPT; ++k)
+      if (in[k] && !have[k]) {
+        st[k].init(p.tab.ids[n0 + k * zstride]);
+        have[k] = true;
       }
-      continue;
-    }
-    // setParticleOnLattice: matching slot, else the first empty one, else drop
-    int slot = -1;
-    if (id[0] == tag)
-      slot = 0;
-    else if (id[1] == tag)
-      slot = 1;
-    else if (id[0] == 0)
-      slot = 0;
-    else if (id[1] == 0)
-      slot = 1;
-    if (slot < 0) continue;
-    float4 nv;
-    nv.x = cd == SF_ONE ? 1.0f : p.sf_value32[cd];
-    // rigid-body velocity of the node (src/LBM_PSM_exchangeParticleData.cpp:83-89)
-    if (im.has_spin) {
-      const float dx = small_int_to_float(hi - im.xi[0]) - im.xf[0];
-      const float dy = small_int_to_float(hj - im.xi[1]) - im.xf[1];
-      const float dz = small_int_to_float(hk - im.xi[2]) - im.xf[2];
-      nv.y = im.uTf[0] + im.omf[1] * dz - im.omf[2] * dy;
-      nv.z = im.uTf[1] + im.omf[2] * dx - im.omf[0] * dz;
-      nv.w = im.uTf[2] + im.omf[0] * dy - im.omf[1] * dx;
+    if (B.w) {
+      const int hi = sx + g.off[0], hj = sy + g.off[1];
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) {
+        if (!in[k]) continue;
+        const int z = sz0 + k * dz;
+        const int hk = z - box_of_z(g, z) * g.bz + g.off[2];  // z in the box's own frame
+        st[k].image(p, n0 + k * zstride, A.w, cd[k], spin_velocity(p.img[ii], hi, hj, hk));
+      }
     } else {
-      nv.y = im.uTf[0];
-      nv.z = im.uTf[1];
-      nv.w = im.uTf[2];
-    }
-    // re-setting a slot to the values it already holds changes nothing
-    bool same = false;
-    if (!slot_dirty[slot] && id[slot] == tag) {
-      if (!have_rec[slot]) {
-        rec[slot] = p.tab.rec32[2 * n + slot];
-        have_rec[slot] = true;
-      }
-      same = __float_as_int(rec[slot].x) == __float_as_int(nv.x) &&
-             __float_as_int(rec[slot].y) == __float_as_int(nv.y) &&
-             __float_as_int(rec[slot].z) == __float_as_int(nv.z) &&
-             __float_as_int(rec[slot].w) == __float_as_int(nv.w);
-    }
-    if (!same) {
-      if (id[slot] != tag) ids_dirty = true;
-      id[slot] = tag;
-      rec[slot] = nv;
-      have_rec[slot] = true;
-      slot_dirty[slot] = true;
+      const int4 U = p.arec[3 * ii + 2];
+      const float4 nv = make_float4(0.f, __int_as_float(U.x), __int_as_float(U.y),
+                                    __int_as_float(U.z));
+#pragma unroll
+      for (int k = 0; k < NPT; ++k)
+        if (in[k]) st[k].image(p, n0 + k * zstride, A.w, cd[k], nv);
     }
   }
-  if (ids_dirty) {
-    p.tab.ids[n] = make_int2(id[0], id[1]);
-    p.tab.flag[n] = (uint8_t)((id[0] > 0 ? 1 : 0) | (id[1] > 0 ? 2 : 0));
-  }
-  if (slot_dirty[0]) p.tab.rec32[2 * n] = rec[0];
-  if (slot_dirty[1]) p.tab.rec32[2 * n + 1] = rec[1];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k)
+    if (have[k]) st[k].store(p, n0 + k * zstride);
 }
 
 cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
@@ -879,10 +952,13 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   sf_shell_kernel<<<p.sm_count * 8, SFS_THREADS, 0, st>>>(p);
   dim3 block(p.cb[0], p.cb[1], p.cb[2]);
   dim3 cells((unsigned)p.C[0], (unsigned)p.C[1], (unsigned)p.C[2]);
-  if (p.write32)
-    node_apply32_kernel<<<cells, block, 0, st>>>(p);
-  else
+  if (p.write32) {
+    constexpr int NPT = 2;  // nodes per thread along z
+    dim3 part(p.cb[0], p.cb[1], (p.cb[2] + NPT - 1) / NPT);
+    node_apply32_kernel<NPT><<<cells, part, 0, st>>>(p);
+  } else {
     node_apply_kernel<<<cells, block, 0, st>>>(p);
+  }
   return cudaGetLastError();
 }
 
