@@ -1094,16 +1094,22 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
       const int k = bx.qlo[2] + q2;
       if (bx.solo && beyond_rP(bx, i, j, k)) continue;
       const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2] + bx.zoff);
+      // both slots' forces are loaded with the ids (no second dependent load)
       const int2 id = p.tab.ids[n];
-      int slot;
-      if (tag == id.x)
-        slot = 0;
-      else if (tag == id.y)
-        slot = 1;
-      else
+      const float2* nf2 = reinterpret_cast<const float2*>(nodeF + 6 * n);
+      const float2 f01 = nf2[0], f23 = nf2[1], f45 = nf2[2];
+      float F0, F1, F2;
+      if (tag == id.x) {
+        F0 = f01.x;
+        F1 = f01.y;
+        F2 = f23.x;
+      } else if (tag == id.y) {
+        F0 = f23.y;
+        F1 = f45.x;
+        F2 = f45.y;
+      } else {
         continue;
-      const float* nf = nodeF + 6 * n + 3 * slot;
-      const float F0 = nf[0], F1 = nf[1], F2 = nf[2];
+      }
       const float dx = small_int_to_float(i - xi[0]) - xf[0];
       const float dy = small_int_to_float(j - xi[1]) - xf[1];
       const float dz = small_int_to_float(k - xi[2]) - xf[2];
