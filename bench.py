@@ -17,7 +17,8 @@ job), but the map is recomputed every step exactly as for moving particles.
 Prints one JSON line on rank 0.  `value` is measured with the particle
 images resident in HBM and the step sequence replayed as a CUDA graph;
 `e2e` runs the same steps through the host-pointer C-ABI call (images copied
-up from pinned memory and forces copied back every step).  The lattice
+up from pinned memory and forces copied back every step; the library replays
+each such step as one CUDA graph).  The lattice
 (1.27 GB in FP32) is ~10x larger than L2, so no L2 flush is needed between
 steps.  `--impl reference` times the CPU oracle (the reference algorithm
 restated in C, FP64, all host cores) on the same workload.
@@ -331,7 +332,8 @@ def run_ours(args, rank=0, world=1):
             "parallelism": f"replicas x{world}",
         },
         "e2e": {"value": round(nodes * K / t_e2e / 1e6, 1), "unit": "MLUPS",
-                "h2d_bytes_per_step": int(n * (4 + 10 * 8)), "d2h_bytes_per_step": int(n * 12 * 8)},
+                "h2d_bytes_per_step": int(n * (4 + 10 * 8)),
+                "d2h_bytes_per_step": int(n * 12 * 8 + 4)},  # F/T/S + the status word
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": f"collide_pipe_kernel<D3Q19,{'float' if args.storage == 'fp32' else '__half'}> "

@@ -70,6 +70,10 @@ struct lbmpsm_handle {
   int last_n = 0;
   // graphs of one step for each parity (map + collide + reduce + bc)
   cudaGraphExec_t gexec[2]{nullptr, nullptr};
+  // graphs of one host-pointer step for each parity (upload of the staged
+  // images, map + collide + reduce, download of the outputs and status word)
+  cudaGraphExec_t hexec[2]{nullptr, nullptr};
+  int hgraph_n = -1;
   PipeConfig pipe{};  // launch shape of the FP32/FP16 collide kernel
   int graph_n = -1;
   int graph_bc = -1;
@@ -253,13 +257,27 @@ void free_particles(lbmpsm_handle* h) {
   h->h_stage_bytes = 0;
 }
 
-void drop_graphs(lbmpsm_handle* h) {
+void drop_run_graphs(lbmpsm_handle* h) {
   for (int k = 0; k < 2; ++k)
     if (h->gexec[k]) {
       cudaGraphExecDestroy(h->gexec[k]);
       h->gexec[k] = nullptr;
     }
   h->graph_n = -1;
+}
+
+void drop_host_graphs(lbmpsm_handle* h) {
+  for (int k = 0; k < 2; ++k)
+    if (h->hexec[k]) {
+      cudaGraphExecDestroy(h->hexec[k]);
+      h->hexec[k] = nullptr;
+    }
+  h->hgraph_n = -1;
+}
+
+void drop_graphs(lbmpsm_handle* h) {
+  drop_run_graphs(h);
+  drop_host_graphs(h);
 }
 
 // cells touched by one image box of width <= w nodes along each axis
@@ -835,10 +853,47 @@ int lbmpsm_set_bc(lbmpsm_handle* h, int bc_type) {
 }  // extern "C"
 
 namespace {
-// Copy one set of particle images (host arrays) to the handle's device
-// buffers through pinned memory; box (may be null) gives each image's box.
+// pinned staging: tags | boxes | x | v | omega | radius (10*cap doubles from
+// x on) | outputs (12*cap doubles) | status word
+struct Stage {
+  int* tag;
+  int* box;
+  double* xvw;
+  double* out;
+  int* status;
+};
+Stage stage_of(const lbmpsm_handle* h) {
+  const size_t cap = (size_t)h->cap;
+  char* st = static_cast<char*>(h->h_stage);
+  const size_t iblk = (sizeof(int) * cap + 15) & ~(size_t)15;
+  Stage s;
+  s.tag = reinterpret_cast<int*>(st);
+  s.box = reinterpret_cast<int*>(st + iblk);
+  s.xvw = reinterpret_cast<double*>(st + 2 * iblk);
+  s.out = s.xvw + 10 * cap;
+  s.status = reinterpret_cast<int*>(s.out + 12 * cap);
+  return s;
+}
+
+// copies of the staged images to the device buffers (enqueued on the stream)
+int upload_images(lbmpsm_handle* h, int n) {
+  if (n <= 0) return LBMPSM_OK;
+  const Stage s = stage_of(h);
+  const size_t nn = (size_t)n;
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_tag, s.tag, sizeof(int) * nn, cudaMemcpyHostToDevice, h->stream));
+  if (h->step_boxes)
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_img_box, s.box, sizeof(int) * nn, cudaMemcpyHostToDevice,
+                                h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw, s.xvw, sizeof(double) * 10 * nn, cudaMemcpyHostToDevice,
+                              h->stream));
+  return LBMPSM_OK;
+}
+
+// Copy one set of particle images (host arrays) into pinned staging and,
+// when upload is set, enqueue their copies to the handle's device buffers;
+// box (may be null) gives each image's box.
 int stage_images(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
-                 const double* v, const double* omega, const double* radius) {
+                 const double* v, const double* omega, const double* radius, bool upload = true) {
   if (box) {
     for (int i = 0; i < n; ++i)
       if (box[i] < 0 || box[i] >= h->nbox)
@@ -853,13 +908,10 @@ int stage_images(lbmpsm_handle* h, int n, const int* box, const int* tag, const 
     return fail(h, LBMPSM_ERR_NUMERIC, "non-finite particle position or radius");
   int rc = ensure_particles(h, n, std::max(rmax, h->opt.max_radius));
   if (rc) return rc;
-  // pinned staging: tags | boxes | x | v | omega | radius | outputs (10*cap doubles after x)
-  const size_t cap = (size_t)h->cap;
-  char* st = static_cast<char*>(h->h_stage);
-  const size_t iblk = (sizeof(int) * cap + 15) & ~(size_t)15;
-  int* stag = reinterpret_cast<int*>(st);
-  int* sbox = reinterpret_cast<int*>(st + iblk);
-  double* sx = reinterpret_cast<double*>(st + 2 * iblk);
+  const Stage sg = stage_of(h);
+  int* stag = sg.tag;
+  int* sbox = sg.box;
+  double* sx = sg.xvw;
   if (h->step_boxes != (box != nullptr)) drop_graphs(h);  // the map reads the boxes or not
   h->step_boxes = box != nullptr;
   if (n > 0) {
@@ -869,44 +921,76 @@ int stage_images(lbmpsm_handle* h, int n, const int* box, const int* tag, const 
     std::memcpy(sx + 3 * nn, v, sizeof(double) * 3 * nn);
     std::memcpy(sx + 6 * nn, omega, sizeof(double) * 3 * nn);
     std::memcpy(sx + 9 * nn, radius, sizeof(double) * nn);
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_tag, stag, sizeof(int) * nn, cudaMemcpyHostToDevice, h->stream));
-    if (box) {
-      std::memcpy(sbox, box, sizeof(int) * nn);
-      CUDA_TRY(h, cudaMemcpyAsync(h->d_img_box, sbox, sizeof(int) * nn, cudaMemcpyHostToDevice,
-                                  h->stream));
-    }
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw, sx, sizeof(double) * 10 * nn, cudaMemcpyHostToDevice,
-                                h->stream));
+    if (box) std::memcpy(sbox, box, sizeof(int) * nn);
   }
-  return LBMPSM_OK;
+  return upload ? upload_images(h, n) : LBMPSM_OK;
 }
 
 // one coupling step with host arrays; box (may be null) gives each image's box
+//
+// The device work of a step with images -- upload of the staged images, map,
+// collide, reduce, download of the outputs and of the status word -- is
+// captured once per A-A parity into a CUDA graph and replayed, so that a
+// step costs one graph launch and one synchronisation on the host.  Steps
+// that store the macroscopic fields run eagerly.
 int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
               const double* v, const double* omega, const double* radius, double* fh, double* th,
               double* stresslet) {
   if (!h || n < 0) return LBMPSM_ERR_ARG;
   if (n > 0 && (!tag || !x || !v || !omega || !radius || !fh || !th || !stresslet))
     return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
-  int rc = stage_images(h, n, box, tag, x, v, omega, radius);
+  int rc = stage_images(h, n, box, tag, x, v, omega, radius, /*upload=*/false);
   if (rc) return rc;
-  const size_t cap = (size_t)h->cap;
-  char* st = static_cast<char*>(h->h_stage);
-  const size_t iblk = (sizeof(int) * cap + 15) & ~(size_t)15;
-  double* out = reinterpret_cast<double*>(st + 2 * iblk) + 10 * cap;
-  rc = enqueue_step(h, n);
-  if (rc) return rc;
-  if (n > 0) {
-    CUDA_TRY(h, cudaMemcpyAsync(out, h->d_out, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost,
-                                h->stream));
-    rc = read_status(h);  // synchronises
+  const Stage sg = stage_of(h);
+  if (n == 0) {
+    rc = enqueue_step(h, n);
     if (rc) return rc;
-    std::memcpy(fh, out, sizeof(double) * 3 * n);
-    std::memcpy(th, out + 3 * n, sizeof(double) * 3 * n);
-    std::memcpy(stresslet, out + 6 * n, sizeof(double) * 6 * n);
-  } else {
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return LBMPSM_OK;
   }
+  const size_t nn = (size_t)n;
+  auto enqueue_all = [&]() -> int {
+    int r = upload_images(h, n);
+    if (!r) r = enqueue_step(h, n);
+    if (r) return r;
+    CUDA_TRY(h, cudaMemcpyAsync(sg.out, h->d_out, sizeof(double) * 12 * nn,
+                                cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(sg.status, h->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                                h->stream));
+    return LBMPSM_OK;
+  };
+  if (h->macro_requested) {
+    rc = enqueue_all();
+    if (rc) return rc;
+  } else {
+    if (h->hgraph_n != n) drop_host_graphs(h);
+    const int par = (int)(h->t & 1);
+    if (!h->hexec[par]) {
+      cudaGraph_t graph;
+      CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      const long long t0 = h->t;
+      rc = enqueue_all();
+      cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+      h->t = t0;  // captured, not run
+      if (rc) return rc;
+      CUDA_TRY(h, ce);
+      cudaError_t ie = cudaGraphInstantiate(&h->hexec[par], graph, 0);
+      cudaGraphDestroy(graph);
+      CUDA_TRY(h, ie);
+      h->hgraph_n = n;
+    }
+    CUDA_TRY(h, cudaGraphLaunch(h->hexec[par], h->stream));
+    h->t += 1;
+    h->last_n = n;
+  }
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (*sg.status) {
+    rc = read_status(h);  // resets the device word and reports the error
+    if (rc) return rc;
+  }
+  std::memcpy(fh, sg.out, sizeof(double) * 3 * nn);
+  std::memcpy(th, sg.out + 3 * nn, sizeof(double) * 3 * nn);
+  std::memcpy(stresslet, sg.out + 6 * nn, sizeof(double) * 6 * nn);
   return LBMPSM_OK;
 }
 }  // namespace
@@ -1084,7 +1168,7 @@ int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps) {
   CUDA_TRY(h, cudaSetDevice(h->device));
   const int n = h->last_n;
   const int use_bc = h->faces.empty() ? 0 : 1;
-  if (h->graph_n != n || h->graph_bc != use_bc || h->macro_requested) drop_graphs(h);
+  if (h->graph_n != n || h->graph_bc != use_bc || h->macro_requested) drop_run_graphs(h);
   // a requested macro store runs eagerly (it changes the kernel arguments)
   while (nsteps > 0 && h->macro_requested) {
     int rc = enqueue_step(h, n);
