@@ -220,23 +220,42 @@ __global__ void img_prep_kernel(MapParams p) {
 }
 
 // Exclusive scan of the cell counts: one block of 1024 threads walking tiles
-// of 4096 counts (4 consecutive per thread), warp shuffles within a tile and
-// a running carry between tiles.
+// of 8192 counts (8 consecutive per thread, two 16-byte loads), warp shuffles
+// within a tile and a running carry between tiles; the offsets go through
+// shared memory so that the stores to global memory are coalesced.
 constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER_THREAD = 8;
 __global__ void __launch_bounds__(SCAN_THREADS) cell_scan_kernel(const int* __restrict__ count,
                                                                  int* __restrict__ off,
                                                                  int ncells) {
+  constexpr int V = SCAN_PER_THREAD;
+  constexpr int TILE = V * SCAN_THREADS;
   __shared__ int wsum[SCAN_THREADS / 32];
   __shared__ int carry_s;
+  __shared__ int tile[TILE + TILE / 32];  // one pad word per 32: conflict-free strided writes
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (t == 0) carry_s = 0;
   __syncthreads();
-  for (int base = 0; base < ncells; base += 4 * SCAN_THREADS) {
-    const int i0 = base + 4 * t;
-    int v[4];
+  for (int base = 0; base < ncells; base += TILE) {
+    const int i0 = base + V * t;
+    int v[V];
+    if (i0 + V <= ncells) {  // i0 is a multiple of 8: aligned 16-byte loads
+      const int4* c4 = reinterpret_cast<const int4*>(count + i0);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] = i0 + k < ncells ? count[i0 + k] : 0;
-    const int own = v[0] + v[1] + v[2] + v[3];
+      for (int k = 0; k < V / 4; ++k) {
+        const int4 w = c4[k];
+        v[4 * k] = w.x;
+        v[4 * k + 1] = w.y;
+        v[4 * k + 2] = w.z;
+        v[4 * k + 3] = w.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < V; ++k) v[k] = i0 + k < ncells ? count[i0 + k] : 0;
+    }
+    int own = 0;
+#pragma unroll
+    for (int k = 0; k < V; ++k) own += v[k];
     int incl = own;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -258,12 +277,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) cell_scan_kernel(const int* __re
     __syncthreads();
     int run = carry_s + wsum[warp] + incl - own;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (i0 + k < ncells) off[i0 + k] = run;
+    for (int k = 0; k < V; ++k) {
+      const int j = V * t + k;
+      tile[j + (j >> 5)] = run;
       run += v[k];
     }
     __syncthreads();
     if (t == SCAN_THREADS - 1) carry_s = run;
+    const int m = min(TILE, ncells - base);
+    for (int j = t; j < m; j += SCAN_THREADS) off[base + j] = tile[j + (j >> 5)];
     __syncthreads();
   }
 }
@@ -944,7 +966,9 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   const int ncells = p.C[0] * p.C[1] * p.C[2];
   const int tb = 128;
   const unsigned wblocks = (unsigned)(((long long)p.n * 32 + tb - 1) / tb);
-  img_prep_kernel<<<(p.n + tb - 1) / tb, tb, 0, st>>>(p);
+  // one warp per block: a thread's image record is a long FP64 chain, so the
+  // images are spread over as many multiprocessors as possible
+  img_prep_kernel<<<(p.n + 31) / 32, 32, 0, st>>>(p);
   cell_scan_kernel<<<1, SCAN_THREADS, 0, st>>>(p.cell_count, p.cell_off, ncells);
   img_fill_kernel<<<wblocks, tb, 0, st>>>(p);
   cell_sort_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(p, ncells);
