@@ -37,6 +37,8 @@ struct lbmpsm_handle {
   long long t = 0;  // LBM steps done
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;                  // cell-list kernels of the map
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   float scale16 = 4096.0f;
   // lattice
   void* f = nullptr;
@@ -445,7 +447,7 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     m.sm_count = h->sm_count;
     m.status = h->d_status;
     m.write32 = h->opt.storage != LBMPSM_STORAGE_FP64 ? 1 : 0;
-    CUDA_TRY(h, launch_map(m, h->stream));
+    CUDA_TRY(h, launch_map(m, h->stream, h->aux, h->ev_fork, h->ev_join));
   }
   int rc = collide(h);
   if (rc) return rc;
@@ -693,7 +695,10 @@ int create_impl(int nbox, const lbmpsm_fix_params* ps, const lbmpsm_options* opt
     return fail(nullptr, rc, "device set-up failed: " + std::string(cudaGetErrorString(cudaGetLastError())));
   };
   if (cudaSetDevice(h->device) != cudaSuccess) return bail(LBMPSM_ERR_CUDA);
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
     return bail(LBMPSM_ERR_CUDA);
   const size_t es = storage_bytes(o.storage);
   const size_t N = (size_t)g.N;
@@ -801,6 +806,10 @@ void lbmpsm_destroy(lbmpsm_handle* h) {
   dfree(h->d_sf_value);
   dfree(h->d_sf_value32);
   dfree(h->d_box);
+  if (h->aux) cudaStreamSynchronize(h->aux);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->aux) cudaStreamDestroy(h->aux);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }

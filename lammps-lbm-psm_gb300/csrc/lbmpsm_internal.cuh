@@ -416,7 +416,10 @@ cudaError_t launch_set_populations(const Geom& g, void* f, int storage, int afte
 cudaError_t launch_check(const Geom& g, const void* f, int storage, int after_odd,
                          float scale16, double* acc4, int* status, cudaStream_t st);
 // particles.cu
-cudaError_t launch_map(const MapParams& p, cudaStream_t st);
+// aux, fork and join (may all be null: one stream) let the cell-list kernels
+// run beside the solid-fraction kernels
+cudaError_t launch_map(const MapParams& p, cudaStream_t st, cudaStream_t aux = nullptr,
+                       cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st);
 cudaError_t launch_table_export(const Geom& g, const Table& t, int* ids, double* eps,
                                 double* us, cudaStream_t st);

@@ -961,7 +961,11 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
     if (have[k]) st[k].store(p, n0 + k * zstride);
 }
 
-cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
+// img_prep; then two independent chains: the cell lists (scan, fill, sort)
+// and the solid fractions (classify, shell); then the table update, which
+// needs both.  With an aux stream the cell-list chain runs there.
+cudaError_t launch_map(const MapParams& p, cudaStream_t st, cudaStream_t aux, cudaEvent_t fork,
+                       cudaEvent_t join) {
   if (p.n <= 0) return cudaSuccess;
   const int ncells = p.C[0] * p.C[1] * p.C[2];
   const int tb = 128;
@@ -969,11 +973,22 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st) {
   // one warp per block: a thread's image record is a long FP64 chain, so the
   // images are spread over as many multiprocessors as possible
   img_prep_kernel<<<(p.n + 31) / 32, 32, 0, st>>>(p);
-  cell_scan_kernel<<<1, SCAN_THREADS, 0, st>>>(p.cell_count, p.cell_off, ncells);
-  img_fill_kernel<<<wblocks, tb, 0, st>>>(p);
-  cell_sort_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(p, ncells);
+  const bool two = aux && fork && join;
+  cudaStream_t cl = two ? aux : st;
+  cudaError_t e;
+  if (two) {
+    if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(aux, fork, 0)) != cudaSuccess) return e;
+  }
+  cell_scan_kernel<<<1, SCAN_THREADS, 0, cl>>>(p.cell_count, p.cell_off, ncells);
+  img_fill_kernel<<<wblocks, tb, 0, cl>>>(p);
+  cell_sort_kernel<<<(ncells + 255) / 256, 256, 0, cl>>>(p, ncells);
   sf_classify_kernel<<<p.n, SFC_THREADS, 0, st>>>(p);
   sf_shell_kernel<<<p.sm_count * 8, SFS_THREADS, 0, st>>>(p);
+  if (two) {
+    if ((e = cudaEventRecord(join, aux)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
+  }
   dim3 block(p.cb[0], p.cb[1], p.cb[2]);
   dim3 cells((unsigned)p.C[0], (unsigned)p.C[1], (unsigned)p.C[2]);
   if (p.write32) {
