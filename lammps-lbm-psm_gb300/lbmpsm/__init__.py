@@ -119,6 +119,11 @@ def load(path: str = LIB_PATH) -> C.CDLL:
                                         C.POINTER(H)]
     lib.lbmpsm_step_batch.argtypes = [H, C.c_int, _I, _I, _D, _D, _D, _D, _D, _D, _D]
     lib.lbmpsm_select_box.argtypes = [H, C.c_int]
+    # the per-step call by raw addresses (its own function object, so that the
+    # typed binding above stays as it is): the cheapest conversion per call
+    _lib_step_addr = lib["lbmpsm_step"]
+    _lib_step_addr.argtypes = [H, C.c_int] + [C.c_void_p] * 8
+    lib.step_by_address = _lib_step_addr
     lib.lbmpsm_adjoint_drag.argtypes = [H, C.c_int, _I, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int,
                                         _D, C.c_int, C.c_double, _D, _D, _D, _D, _D]
     lib.lbmpsm_tangent_drag.argtypes = [H, C.c_int, _I, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int,
@@ -209,10 +214,12 @@ class Lattice:
         v = np.ascontiguousarray(v, dtype=np.float64).reshape(n, 3)
         omega = np.ascontiguousarray(omega, dtype=np.float64).reshape(n, 3)
         radius = np.ascontiguousarray(radius, dtype=np.float64).reshape(n)
-        fh = np.zeros((n, 3)); th = np.zeros((n, 3)); S = np.zeros((n, 6))
-        self._check(self.lib.lbmpsm_step(self.h, n, _p(tag, _I), _p(x), _p(v), _p(omega),
-                                         _p(radius), _p(fh), _p(th), _p(S)))
-        return fh, th, S
+        out = np.empty(12 * n)  # fh | th | S, every element written by the call
+        a = out.ctypes.data
+        self._check(self.lib.step_by_address(
+            self.h, n, tag.ctypes.data, x.ctypes.data, v.ctypes.data, omega.ctypes.data,
+            radius.ctypes.data, a, a + 24 * n, a + 48 * n))
+        return out[:3 * n].reshape(n, 3), out[3 * n:6 * n].reshape(n, 3), out[6 * n:].reshape(n, 6)
 
     @staticmethod
     def _images(tag, x, v, omega, radius):
