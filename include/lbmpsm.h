@@ -64,6 +64,20 @@ extern "C" {
 #define LBMPSM_WEIGHT_REFERENCE 0 /* B_n = eps_n, renormalised when sum > 1 (reference) */
 #define LBMPSM_WEIGHT_NOBLE_TORCZYNSKI 1 /* B_n = eps_n(tau-1/2)/((1-eps_n)+(tau-1/2)) */
 
+/* Launch shape of the FP32/FP16 collide kernel (no reference counterpart).
+ * AUTO: at the start of the second step (the first step's map has filled the
+ * particle table) the library times every candidate -- the row pipeline with
+ * 3, 2, 4 or 5 shared-memory stages -- for a few even/odd step pairs on a
+ * scratch copy of the populations and keeps the fastest (a few milliseconds,
+ * one temporary population-sized allocation; skipped, and retried on the next
+ * step, while the stream is being captured; the default shape is kept if the
+ * allocation fails).  The candidates give bit-identical results.  DEFAULT:
+ * the 3-stage pipeline, untimed.  The environment variable LBMPSM_PIPE_STAGES
+ * (2..5 stages, or 0 = the direct kernel, which rows longer than 256 nodes
+ * use anyway) overrides both. */
+#define LBMPSM_TUNE_AUTO 0
+#define LBMPSM_TUNE_DEFAULT 1
+
 typedef struct lbmpsm_handle lbmpsm_handle;
 
 /* Arguments of `fix lbm-psm` (src/fix_LBM_PSM.cpp:15-83) plus the LAMMPS
@@ -89,6 +103,7 @@ typedef struct {
   double max_radius; /* largest particle radius, physical units (0: derived per call on
                         host-pointer calls; required for *_device calls) */
   int psm_weighting; /* LBMPSM_WEIGHT_* */
+  int collide_tuning; /* LBMPSM_TUNE_*: how the FP32/FP16 collide kernel's launch shape is chosen */
 } lbmpsm_options;
 
 /* Derived quantities of fix_LBM_PSM::init and UnitConversion
@@ -105,6 +120,11 @@ typedef struct {
   double F_lbm[3];       /* lattice-unit body force */
   int64_t steps;         /* LBM steps done on this handle */
   size_t device_bytes;   /* device memory held by the handle */
+  int collide_stages;    /* FP32/FP16 collide launch shape: pipeline stages, 0 = direct kernel
+                            (-1 for FP64 storage) */
+  int collide_blocks;    /* its grid (persistent blocks; 0 for the direct kernel) */
+  float collide_tune_ms[4]; /* autotuner: ms per even+odd step pair of the shapes with 3, 2,
+                            4 and 5 stages (-1: not timed or not fitting) */
 } lbmpsm_info;
 
 /* Replaces fix_LBM_PSM::init (src/fix_LBM_PSM.cpp:104-177): unit conversion,

@@ -77,6 +77,8 @@ struct lbmpsm_handle {
   cudaGraphExec_t hexec[2]{nullptr, nullptr};
   int hgraph_n = -1;
   PipeConfig pipe{};  // launch shape of the FP32/FP16 collide kernel
+  float tune_ms[LBMPSM_TUNE_CANDIDATES] = {-1.f, -1.f, -1.f, -1.f};
+  bool tune_pending = false;  // the collide autotuner has yet to run
   int graph_n = -1;
   int graph_bc = -1;
   size_t dev_bytes = 0;
@@ -398,6 +400,51 @@ int collide(lbmpsm_handle* h) {
     h->macro_valid = true;
   }
   h->t += 1;
+  return LBMPSM_OK;
+}
+
+// The collide autotuner (lbmpsm_options.collide_tuning): once the table
+// holds the particles (from the second step on), every candidate launch shape
+// runs a few even/odd step pairs on a scratch copy of the populations and the
+// fastest is kept; the step graphs are rebuilt with it.  Skipped while the
+// stream is being captured (it synchronises) and when the scratch copy cannot
+// be allocated.  The trial collides write node forces, which the step's own
+// collide rewrites for every node that holds a particle.
+int maybe_tune(lbmpsm_handle* h) {
+  if (!h->tune_pending || h->t < 1) return LBMPSM_OK;
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CUDA_TRY(h, cudaStreamIsCapturing(h->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return LBMPSM_OK;
+  h->tune_pending = false;
+  void* scratch = nullptr;
+  const size_t bytes = storage_bytes(h->opt.storage) * (size_t)h->g.Np * h->g.Q;
+  if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return LBMPSM_OK;
+  }
+  CollideParams p{};
+  p.g = h->g;
+  p.f = scratch;
+  p.tab = h->tab;
+  p.weighting = h->opt.psm_weighting;
+  p.box = h->d_box;
+  p.has_force = h->any_force ? 1 : 0;
+  p.invCs2 = h->invCs2;
+  p.invCs4 = h->invCs4;
+  p.scale16 = h->scale16;
+  p.status = h->d_status;
+  PipeConfig best = h->pipe;
+  cudaError_t e = cudaMemcpyAsync(scratch, h->f, bytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess) e = tune_collide_lowp(p, h->opt.storage, h->sm_count, h->stream, &best, h->tune_ms);
+  cudaStreamSynchronize(h->stream);
+  cudaFree(scratch);
+  CUDA_TRY(h, e);
+  CUDA_TRY(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+  if (best.grid != h->pipe.grid || best.stages != h->pipe.stages) {
+    h->pipe = best;
+    drop_graphs(h);
+  }
   return LBMPSM_OK;
 }
 
@@ -755,11 +802,15 @@ int create_impl(int nbox, const lbmpsm_fix_params* ps, const lbmpsm_options* opt
     return bail(LBMPSM_ERR_CUDA);
   h->sm_count = std::max(sms, 1);
   if (o.storage != LBMPSM_STORAGE_FP64) {
-    // persistent row pipeline: stage count from LBMPSM_PIPE_STAGES (3, 4 or 5; default 3)
+    // launch shape of the collide kernel: LBMPSM_PIPE_STAGES if set (0 = direct
+    // kernel, 2..5 stages), else the autotuner or the 3-stage default
     const char* env = std::getenv("LBMPSM_PIPE_STAGES");
     const int stages = env ? std::atoi(env) : 3;
     if (prepare_collide_lowp(g, o.storage, sms, stages, &h->pipe) != cudaSuccess)
       return bail(LBMPSM_ERR_CUDA);
+    // the autotuner runs at the start of the second step, when the first
+    // step's map has filled the particle table
+    h->tune_pending = !env && o.collide_tuning == LBMPSM_TUNE_AUTO;
   }
   int rc = ensure_particles(h, std::max(o.max_images, 1), o.max_radius > 0 ? o.max_radius : 8.0 * h->dx);
   if (rc) {
@@ -838,6 +889,9 @@ int lbmpsm_get_info(const lbmpsm_handle* h, lbmpsm_info* info) {
   for (int d = 0; d < 3; ++d) info->F_lbm[d] = h->F_lbm[d];
   info->steps = h->t;
   info->device_bytes = h->dev_bytes;
+  info->collide_stages = h->opt.storage == LBMPSM_STORAGE_FP64 ? -1 : (h->pipe.grid > 0 ? h->pipe.stages : 0);
+  info->collide_blocks = h->pipe.grid;
+  for (int k = 0; k < LBMPSM_TUNE_CANDIDATES; ++k) info->collide_tune_ms[k] = h->tune_ms[k];
   return LBMPSM_OK;
 }
 
@@ -948,7 +1002,9 @@ int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const dou
   if (!h || n < 0) return LBMPSM_ERR_ARG;
   if (n > 0 && (!tag || !x || !v || !omega || !radius || !fh || !th || !stresslet))
     return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
-  int rc = stage_images(h, n, box, tag, x, v, omega, radius, /*upload=*/false);
+  int rc = maybe_tune(h);
+  if (rc) return rc;
+  rc = stage_images(h, n, box, tag, x, v, omega, radius, /*upload=*/false);
   if (rc) return rc;
   const Stage sg = stage_of(h);
   if (n == 0) {
@@ -1029,6 +1085,10 @@ int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
   if (h->nbox > 1 && n > 0)
     return fail(h, LBMPSM_ERR_ARG, "an ensemble needs the box of every image (lbmpsm_step_batch)");
   CUDA_TRY(h, cudaSetDevice(h->device));
+  {
+    const int trc = maybe_tune(h);
+    if (trc) return trc;
+  }
   if (h->step_boxes) drop_graphs(h);
   h->step_boxes = false;
   const size_t nn = (size_t)n;
@@ -1175,6 +1235,10 @@ void* lbmpsm_stream(lbmpsm_handle* h) { return h ? (void*)h->stream : nullptr; }
 int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps) {
   if (!h || nsteps < 0) return LBMPSM_ERR_ARG;
   CUDA_TRY(h, cudaSetDevice(h->device));
+  {
+    const int trc = maybe_tune(h);
+    if (trc) return trc;
+  }
   const int n = h->last_n;
   const int use_bc = h->faces.empty() ? 0 : 1;
   if (h->graph_n != n || h->graph_bc != use_bc || h->macro_requested) drop_run_graphs(h);

@@ -591,6 +591,8 @@ static cudaError_t prepare_lowp(const Geom& g, int sm_count, int stages, PipeCon
   *cfg = PipeConfig{};
   if (g.S[0] > STAGED_MAX_ROW) return cudaSuccess;
   switch (stages) {
+    case 0: return cudaSuccess;  // the direct kernel
+    case 2: return pipe_prepare<L, T, 2, 3>(g, sm_count, cfg);
     case 4: return pipe_prepare<L, T, 4, 2>(g, sm_count, cfg);
     case 5: return pipe_prepare<L, T, 5, 2>(g, sm_count, cfg);
     default: return pipe_prepare<L, T, 3, 3>(g, sm_count, cfg);
@@ -626,6 +628,7 @@ template <class L, typename T>
 static cudaError_t launch_lowp(const CollideParams& p, int odd, cudaStream_t st) {
   if (p.pipe.grid > 0) {
     switch (p.pipe.stages) {
+      case 2: launch_pipe<L, T, 2, 3>(p, odd, st); break;
       case 4: launch_pipe<L, T, 4, 2>(p, odd, st); break;
       case 5: launch_pipe<L, T, 5, 2>(p, odd, st); break;
       default: launch_pipe<L, T, 3, 3>(p, odd, st); break;
@@ -646,6 +649,64 @@ static cudaError_t launch_lowp(const CollideParams& p, int odd, cudaStream_t st)
       collide_lowp_kernel<L, T, false, false><<<grid, block, 0, st>>>(p);
   }
   return cudaGetLastError();
+}
+
+// The project's autotuner for the FP32/FP16 collide: every candidate launch
+// shape -- the row pipeline with 3, 2, 4 or 5 stages, each at the blocks per
+// multiprocessor its shared memory and registers allow -- runs a few even/odd
+// step pairs on p.f (a scratch copy of the populations), timed with CUDA
+// events on the stream; the fastest is kept.  The candidates are one template
+// (only the stage count and the launch bounds differ), so they round alike
+// and the choice changes speed only, never results.  The direct kernel (the
+// fallback for rows longer than one staged block) is not a candidate: it
+// inlines the same node arithmetic into another kernel, where the compiler's
+// multiply-add contraction may round differently.
+cudaError_t tune_collide_lowp(CollideParams p, int storage, int sm_count, cudaStream_t st,
+                              PipeConfig* best, float* ms_out) {
+  const int cand[LBMPSM_TUNE_CANDIDATES] = {3, 2, 4, 5};
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaEventCreate(&e1)) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return e;
+  }
+  float best_ms = 0.0f;
+  bool have = false;
+  for (int k = 0; k < LBMPSM_TUNE_CANDIDATES; ++k) {
+    ms_out[k] = -1.0f;
+    PipeConfig c{};
+    if (cand[k] > 0) {
+      if ((e = prepare_collide_lowp(p.g, storage, sm_count, cand[k], &c)) != cudaSuccess) break;
+      if (c.grid == 0) continue;  // this shape does not fit the lattice's rows
+    }
+    p.pipe = c;
+    auto pair = [&]() {
+      for (int odd = 0; odd < 2; ++odd)
+        if (storage == 1)
+          launch_collide_f32(p, odd, st);
+        else
+          launch_collide_f16(p, odd, st);
+    };
+    pair();  // warm-up
+    cudaEventRecord(e0, st);
+    constexpr int REPS = 3;
+    for (int r = 0; r < REPS; ++r) pair();
+    cudaEventRecord(e1, st);
+    if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms_out[k] = ms / REPS;
+    if (!have || ms_out[k] < best_ms) {
+      best_ms = ms_out[k];
+      *best = c;
+      have = true;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return e;
 }
 
 cudaError_t launch_collide_f32(const CollideParams& p, int odd, cudaStream_t st) {

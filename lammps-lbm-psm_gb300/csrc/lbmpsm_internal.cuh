@@ -400,9 +400,16 @@ cudaError_t launch_collide_f64(const CollideParams& p, int odd, cudaStream_t st)
 cudaError_t launch_collide_f32(const CollideParams& p, int odd, cudaStream_t st);
 cudaError_t launch_collide_f16(const CollideParams& p, int odd, cudaStream_t st);
 // storage 1 (FP32) or 2 (FP16); sets the kernels' shared-memory limit and
-// sizes the persistent grid from the occupancy on this device
+// sizes the persistent grid from the occupancy on this device (stages 0:
+// the direct kernel, cfg left empty)
 cudaError_t prepare_collide_lowp(const Geom& g, int storage, int sm_count, int stages,
                                  PipeConfig* cfg);
+// times the candidate launch shapes (pipeline stages 3, 2, 4, 5) on p.f and
+// stores the fastest in best (unchanged if none fits), the per-pair times in
+// ms_out (-1: shape does not fit)
+constexpr int LBMPSM_TUNE_CANDIDATES = 4;
+cudaError_t tune_collide_lowp(CollideParams p, int storage, int sm_count, cudaStream_t st,
+                              PipeConfig* best, float* ms_out);
 cudaError_t launch_bc_f64(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f32(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f16(const BCParams& p, cudaStream_t st);

@@ -31,6 +31,7 @@ ERR_ARG, ERR_MACH, ERR_GRID, ERR_NOMEM, ERR_CUDA, ERR_STATE, ERR_CAPACITY, ERR_N
 STORAGE = {"fp64": 0, "fp32": 1, "fp16": 2}
 BC = {"none": 0, "shear": 1, "xFlow": 2, "channel": 3, "channel-velIn-pressOut": 4, "closedBox": 5}
 WEIGHTING = {"reference": 0, "noble-torczynski": 1}
+TUNING = {"auto": 0, "default": 1}  # LBMPSM_TUNE_*
 
 SYMBOLS = (
     "lbmpsm_create", "lbmpsm_destroy", "lbmpsm_last_error", "lbmpsm_get_info", "lbmpsm_set_bc",
@@ -61,7 +62,7 @@ class FixParams(C.Structure):
 class Options(C.Structure):
     _fields_ = [
         ("storage", C.c_int), ("device", C.c_int), ("max_images", C.c_int),
-        ("max_radius", C.c_double), ("psm_weighting", C.c_int),
+        ("max_radius", C.c_double), ("psm_weighting", C.c_int), ("collide_tuning", C.c_int),
     ]
 
 
@@ -73,6 +74,7 @@ class Info(C.Structure):
         ("dt_d", C.c_double), ("forceFactor", C.c_double), ("torqueFactor", C.c_double),
         ("volumeForceFactor", C.c_double), ("dt_dem", C.c_double), ("Ma", C.c_double),
         ("F_lbm", C.c_double * 3), ("steps", C.c_int64), ("device_bytes", C.c_size_t),
+        ("collide_stages", C.c_int), ("collide_blocks", C.c_int), ("collide_tune_ms", C.c_float * 4),
     ]
 
 
@@ -143,7 +145,7 @@ class Lattice:
                  nevery: int = 1, Nlc: int, lc: float, rho: float = 1.0, nu: float, Re: float,
                  tau: float = 0.7, Fext=(0.0, 0.0, 0.0), storage: str = "fp64", device: int = 0,
                  max_images: int = 0, max_radius: float = 0.0, weighting: str = "reference",
-                 bc: str | int = "none"):
+                 bc: str | int = "none", collide_tuning: str = "auto"):
         self.lib = load()
         p = FixParams()
         p.dimension = dimension
@@ -158,6 +160,7 @@ class Lattice:
         o.max_images = max_images
         o.max_radius = max_radius
         o.psm_weighting = WEIGHTING[weighting]
+        o.collide_tuning = TUNING[collide_tuning]
         h = C.c_void_p()
         rc = self.lib.lbmpsm_create(C.byref(p), C.byref(o), C.byref(h))
         if rc != OK:
@@ -357,7 +360,8 @@ class Ensemble(Lattice):
     particle_table) address the box chosen with :meth:`select_box`."""
 
     def __init__(self, boxes, *, storage: str = "fp64", device: int = 0, max_images: int = 0,
-                 max_radius: float = 0.0, weighting: str = "reference"):
+                 max_radius: float = 0.0, weighting: str = "reference",
+                 collide_tuning: str = "auto"):
         self.lib = load()
         n = len(boxes)
         arr = (FixParams * n)(*[_fix_params(**b) for b in boxes])
@@ -367,6 +371,7 @@ class Ensemble(Lattice):
         o.max_images = max_images
         o.max_radius = max_radius
         o.psm_weighting = WEIGHTING[weighting]
+        o.collide_tuning = TUNING[collide_tuning]
         h = C.c_void_p()
         rc = self.lib.lbmpsm_create_batch(n, arr, C.byref(o), C.byref(h))
         if rc != OK:
