@@ -258,6 +258,25 @@ int lbmpsm_select_box(lbmpsm_handle* h, int box);
 int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, double B0, double rho0,
                                 double u0, void* solid, void* rho, void* u);
 
+/* Groups of lattices stepped together (no reference counterpart).  Boxes of
+ * one geometry share an ensemble handle (lbmpsm_create_batch); boxes of other
+ * sizes need their own handles.  A group advances several handles as one:
+ * lbmpsm_group_run_fixed runs nsteps steps of every member exactly as
+ * lbmpsm_run_fixed would (each with the images it holds from its last step,
+ * each with its boundary condition), with one step of all members captured
+ * once per A-A parity into a single CUDA graph whose branches run
+ * concurrently, so that every step is one graph launch.  Members must be on
+ * one device and at the same step parity; a member with a macro-field store
+ * pending is rejected (LBMPSM_ERR_STATE).  The group's work is ordered after
+ * the members' earlier work and before their later work.  Destroy the group
+ * before its members. */
+typedef struct lbmpsm_group lbmpsm_group;
+int lbmpsm_group_create(lbmpsm_handle* const* handles, int count, lbmpsm_group** out);
+int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps);
+void* lbmpsm_group_stream(lbmpsm_group* g); /* the cudaStream_t the group's graphs run on */
+const char* lbmpsm_group_last_error(const lbmpsm_group* g);
+void lbmpsm_group_destroy(lbmpsm_group* g);
+
 /* Sensitivities of the time-averaged drag (the reference has
  * no adjoint; the forward step is lbmpsm_step's).  Both calls run nsteps
  * ordinary coupling steps with one fixed set of particle images -- exactly

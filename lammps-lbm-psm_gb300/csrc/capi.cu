@@ -81,6 +81,7 @@ struct lbmpsm_handle {
   bool tune_pending = false;  // the collide autotuner has yet to run
   int graph_n = -1;
   int graph_bc = -1;
+  long long graph_gen = 0;  // bumped whenever captured graphs become stale (groups check it)
   size_t dev_bytes = 0;
   std::string err;
   // batched ensemble: nbox boxes stacked along z (one lattice: nbox = 1)
@@ -282,6 +283,7 @@ void drop_host_graphs(lbmpsm_handle* h) {
 void drop_graphs(lbmpsm_handle* h) {
   drop_run_graphs(h);
   drop_host_graphs(h);
+  h->graph_gen += 1;
 }
 
 // cells touched by one image box of width <= w nodes along each axis
@@ -1724,6 +1726,174 @@ int lbmpsm_tangent_drag(lbmpsm_handle* h, int n, const int* tag, const double* x
   for (int t = t0; t <= t1; ++t) sJ += hd[(size_t)(t - 1)];
   if (J) *J = sJ / (double)(t1 - t0 + 1);
   if (dJ) *dJ = hs[0];
+  return LBMPSM_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Groups of lattices stepped as one CUDA graph (lbmpsm_group_*).
+//
+// A batched ensemble holds boxes of one lattice geometry; boxes of different
+// sizes form separate handles.  A group advances several handles together:
+// one step of every member (map, collide, reduce, boundary condition, each
+// on the member's own streams as lbmpsm_run_fixed would run it) is captured
+// once per A-A parity into a single graph whose branches run concurrently,
+// so that all members take one graph launch per step.
+struct lbmpsm_group {
+  std::vector<lbmpsm_handle*> hs;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t gexec[2]{nullptr, nullptr};
+  std::vector<long long> gen;  // members' graph generations the graphs were captured at
+  std::vector<int> cap_n, cap_bc;
+  std::string err;
+};
+
+namespace {
+int gfail(lbmpsm_group* g, int code, const std::string& msg) {
+  g->err = msg;
+  return code;
+}
+#define GROUP_TRY(g, call)                                                                  \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return gfail((g), LBMPSM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+void group_drop(lbmpsm_group* g) {
+  for (int k = 0; k < 2; ++k)
+    if (g->gexec[k]) {
+      cudaGraphExecDestroy(g->gexec[k]);
+      g->gexec[k] = nullptr;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int lbmpsm_group_create(lbmpsm_handle* const* handles, int count, lbmpsm_group** out) {
+  if (!out) return LBMPSM_ERR_ARG;
+  *out = nullptr;
+  if (!handles || count < 1) return fail(nullptr, LBMPSM_ERR_ARG, "a group needs at least one lattice");
+  for (int i = 0; i < count; ++i) {
+    if (!handles[i]) return fail(nullptr, LBMPSM_ERR_ARG, "NULL lattice in a group");
+    if (handles[i]->device != handles[0]->device)
+      return fail(nullptr, LBMPSM_ERR_ARG, "the lattices of a group must be on one device");
+    for (int j = 0; j < i; ++j)
+      if (handles[j] == handles[i])
+        return fail(nullptr, LBMPSM_ERR_ARG, "a lattice appears twice in a group");
+  }
+  lbmpsm_group* g = new (std::nothrow) lbmpsm_group();
+  if (!g) return fail(nullptr, LBMPSM_ERR_NOMEM, "host allocation failed");
+  g->hs.assign(handles, handles + count);
+  g->device = handles[0]->device;
+  g->join.assign((size_t)count, nullptr);
+  bool ok = cudaSetDevice(g->device) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming) == cudaSuccess;
+  for (auto& e : g->join) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    lbmpsm_group_destroy(g);
+    return fail(nullptr, LBMPSM_ERR_CUDA, "group set-up failed");
+  }
+  *out = g;
+  return LBMPSM_OK;
+}
+
+void lbmpsm_group_destroy(lbmpsm_group* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  group_drop(g);
+  for (auto e : g->join)
+    if (e) cudaEventDestroy(e);
+  if (g->fork) cudaEventDestroy(g->fork);
+  if (g->done) cudaEventDestroy(g->done);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+
+const char* lbmpsm_group_last_error(const lbmpsm_group* g) { return g ? g->err.c_str() : ""; }
+
+void* lbmpsm_group_stream(lbmpsm_group* g) { return g ? (void*)g->stream : nullptr; }
+
+int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps) {
+  if (!g || nsteps < 0) return LBMPSM_ERR_ARG;
+  GROUP_TRY(g, cudaSetDevice(g->device));
+  const size_t m = g->hs.size();
+  const long long par0 = g->hs[0]->t & 1;
+  for (size_t i = 0; i < m; ++i) {
+    lbmpsm_handle* h = g->hs[i];
+    if ((h->t & 1) != par0)
+      return gfail(g, LBMPSM_ERR_STATE, "the lattices of a group must be at the same step parity");
+    if (h->macro_requested)
+      return gfail(g, LBMPSM_ERR_STATE, "a member has a macro-field store pending (use lbmpsm_run_fixed)");
+    const int rc = maybe_tune(h);
+    if (rc) return gfail(g, rc, h->err);
+  }
+  // the graphs are stale if a member's buffers, images or boundary condition changed
+  bool stale = g->gen.size() != m;
+  for (size_t i = 0; !stale && i < m; ++i) {
+    const lbmpsm_handle* h = g->hs[i];
+    stale = g->gen[i] != h->graph_gen || g->cap_n[i] != h->last_n ||
+            g->cap_bc[i] != (h->faces.empty() ? 0 : 1);
+  }
+  if (stale) group_drop(g);
+  // order after the members' earlier work
+  for (size_t i = 0; i < m; ++i) {
+    GROUP_TRY(g, cudaEventRecord(g->join[i], g->hs[i]->stream));
+    GROUP_TRY(g, cudaStreamWaitEvent(g->stream, g->join[i], 0));
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    const int par = (int)(g->hs[0]->t & 1);
+    if (!g->gexec[par]) {
+      cudaGraph_t graph = nullptr;
+      std::vector<long long> t0(m);
+      for (size_t i = 0; i < m; ++i) t0[i] = g->hs[i]->t;
+      GROUP_TRY(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = LBMPSM_OK;
+      cudaError_t ce = cudaEventRecord(g->fork, g->stream);
+      for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
+        lbmpsm_handle* h = g->hs[i];
+        ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
+        if (ce != cudaSuccess) break;
+        rc = enqueue_step(h, h->last_n);
+        if (!rc && !h->faces.empty()) rc = enqueue_bc(h);
+        if (rc) rc = gfail(g, rc, h->err);
+        if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
+        if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
+      }
+      cudaError_t ee = cudaStreamEndCapture(g->stream, &graph);
+      for (size_t i = 0; i < m; ++i) g->hs[i]->t = t0[i];  // captured, not run
+      if (rc || ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (rc) return rc;
+        GROUP_TRY(g, ce);
+        GROUP_TRY(g, ee);
+      }
+      cudaError_t ie = cudaGraphInstantiate(&g->gexec[par], graph, 0);
+      cudaGraphDestroy(graph);
+      GROUP_TRY(g, ie);
+      g->gen.resize(m);
+      g->cap_n.resize(m);
+      g->cap_bc.resize(m);
+      for (size_t i = 0; i < m; ++i) {
+        g->gen[i] = g->hs[i]->graph_gen;
+        g->cap_n[i] = g->hs[i]->last_n;
+        g->cap_bc[i] = g->hs[i]->faces.empty() ? 0 : 1;
+      }
+    }
+    GROUP_TRY(g, cudaGraphLaunch(g->gexec[par], g->stream));
+    for (size_t i = 0; i < m; ++i) g->hs[i]->t += 1;
+  }
+  // the members' later work is ordered after the group's
+  GROUP_TRY(g, cudaEventRecord(g->done, g->stream));
+  for (size_t i = 0; i < m; ++i) GROUP_TRY(g, cudaStreamWaitEvent(g->hs[i]->stream, g->done, 0));
   return LBMPSM_OK;
 }
 

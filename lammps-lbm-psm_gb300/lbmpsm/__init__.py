@@ -41,6 +41,8 @@ SYMBOLS = (
     "lbmpsm_run_fixed", "lbmpsm_read_forces", "lbmpsm_export_fields_static",
     "lbmpsm_create_batch", "lbmpsm_step_batch", "lbmpsm_select_box",
     "lbmpsm_adjoint_drag", "lbmpsm_tangent_drag",
+    "lbmpsm_group_create", "lbmpsm_group_run_fixed", "lbmpsm_group_stream",
+    "lbmpsm_group_last_error", "lbmpsm_group_destroy",
 )
 
 
@@ -130,6 +132,14 @@ def load(path: str = LIB_PATH) -> C.CDLL:
                                         _D, C.c_int, C.c_double, _D, _D, _D, _D, _D]
     lib.lbmpsm_tangent_drag.argtypes = [H, C.c_int, _I, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int,
                                         _D, C.c_double, C.c_double, _D, _D, _D, _D]
+    lib.lbmpsm_group_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]
+    lib.lbmpsm_group_run_fixed.argtypes = [H, C.c_int]
+    lib.lbmpsm_group_stream.argtypes = [H]
+    lib.lbmpsm_group_stream.restype = C.c_void_p
+    lib.lbmpsm_group_last_error.argtypes = [H]
+    lib.lbmpsm_group_last_error.restype = C.c_char_p
+    lib.lbmpsm_group_destroy.argtypes = [H]
+    lib.lbmpsm_group_destroy.restype = None
     _lib = lib
     return lib
 
@@ -402,3 +412,39 @@ class Ensemble(Lattice):
                                                _p(omega), _p(radius), _p(fh), _p(th), _p(S)))
         return fh, th, S
 
+
+
+class Group:
+    """Several lattices / ensembles (e.g. one per box size) advanced together:
+    one CUDA graph launch per step for all members (lbmpsm_group_*).  Destroy
+    (close) the group before its members."""
+
+    def __init__(self, members):
+        self.lib = load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        g = C.c_void_p()
+        rc = self.lib.lbmpsm_group_create(arr, len(self.members), C.byref(g))
+        if rc != OK:
+            raise LbmPsmError(rc, self.lib.lbmpsm_last_error(None).decode())
+        self.g = g
+
+    def run_fixed(self, nsteps: int):
+        rc = self.lib.lbmpsm_group_run_fixed(self.g, int(nsteps))
+        if rc != OK:
+            raise LbmPsmError(rc, self.lib.lbmpsm_group_last_error(self.g).decode())
+
+    @property
+    def stream(self) -> int:
+        return self.lib.lbmpsm_group_stream(self.g)
+
+    def close(self):
+        if getattr(self, "g", None):
+            self.lib.lbmpsm_group_destroy(self.g)
+            self.g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

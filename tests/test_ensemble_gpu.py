@@ -90,3 +90,76 @@ def test_ensemble_rejects_mixed_geometry_and_boundary_conditions():
     assert e.value.code == lbmpsm.ERR_STATE
     with pytest.raises(lbmpsm.LbmPsmError):
         ens.select_box(3)
+
+
+def test_group_of_ensembles_of_different_sizes_equals_separate_runs():
+    """Boxes of two sizes (an ensemble of 20^3 boxes, one of 16^3 boxes) and a
+    plain lattice stepped as one group -- one graph launch per step -- give the
+    same populations and forces as each advanced on its own."""
+    def make(edge, seed):
+        boxes = []
+        for b, tau in enumerate((0.7, 0.85)):
+            nu = (tau - 0.5) / 3.0
+            boxes.append(dict(dimension=3, prd=(float(edge),) * 3, periodic=(1, 1, 1), Nlc=9,
+                              lc=8.0, rho=1.0, nu=nu, Re=0.01 * 8 / nu, tau=tau,
+                              Fext=(2e-6 * (b + 1), 0.0, 0.0)))
+        imgs, bidx = [], []
+        for b, box in enumerate(boxes):
+            rng = np.random.default_rng(seed + b)
+            x, r = cases.rsa(rng, 2, (4.0, 6.0), np.zeros(3), np.full(3, float(edge)), 3,
+                             min_gap=0.5)
+            n = len(x)
+            g = cases.product_make_ghosts(3, (0.0, 0.0, 0.0), box["prd"], (1, 1, 1), 6.0,
+                                          np.arange(1, n + 1), x, np.zeros((n, 3)),
+                                          np.zeros((n, 3)), r)
+            imgs.append(g)
+            bidx.append(np.full(len(g["tag"]), b, np.int32))
+        cat = {k: np.concatenate([g[k] for g in imgs]) for k in ("tag", "x", "v", "omega", "radius")}
+        return boxes, np.concatenate(bidx), cat
+
+    def setup():
+        members, nimg = [], []
+        for edge, seed in ((20, 7), (16, 9)):
+            boxes, bidx, cat = make(edge, seed)
+            ens = lbmpsm.Ensemble(boxes, storage="fp32")
+            ens.step(bidx, cat["tag"], cat["x"], cat["v"], cat["omega"], cat["radius"])
+            members.append(ens)
+            nimg.append(len(cat["tag"]))
+        case = cases.CASES["c2_sphere_3d"]
+        lat = lbmpsm.Lattice(**case.params(), storage="fp32")
+        tag, x, v, w, r = cases.initial_particles(case)
+        g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
+        lat.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+        members.append(lat)
+        nimg.append(len(g["tag"]))
+        return members, nimg
+
+    solo, nimg = setup()
+    for m in solo:
+        m.run_fixed(9)
+    grouped, _ = setup()
+    grp = lbmpsm.Group(grouped)
+    grp.run_fixed(4)
+    grp.run_fixed(5)
+    grp.close()
+    for a, b, n in zip(solo, grouped, nimg):
+        assert a.steps == b.steps == 10
+        fa, fb = a.read_forces(n), b.read_forces(n)
+        assert np.abs(fa[0]).max() > 0
+        for u, w in zip(fa, fb):
+            assert np.array_equal(u, w)
+        nb = getattr(a, "nbox", 1)
+        for box in range(nb):
+            if nb > 1:
+                a.select_box(box)
+                b.select_box(box)
+            m = a.stored_mask()
+            assert np.array_equal(a.populations()[m], b.populations()[m])
+    # members at different step parities are rejected
+    odd, _ = setup()
+    odd[0].run_fixed(1)
+    grp = lbmpsm.Group(odd)
+    with pytest.raises(lbmpsm.LbmPsmError) as e:
+        grp.run_fixed(1)
+    assert e.value.code == lbmpsm.ERR_STATE
+    grp.close()
