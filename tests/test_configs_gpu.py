@@ -1,4 +1,4 @@
-"""The BASELINE parity configurations at their full sizes.
+"""The parity configurations at their full sizes.
 
 * C1: D2Q9 256 x 256 periodic, tau 0.65, Guo force (1e-6, 0), one fixed disc
   of diameter 16 at the centre, plain FP64, 5000 steps: the GPU path against
