@@ -69,7 +69,27 @@ def build(force: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_driver(force)
     return LIB
+
+
+HOST = os.path.join(PKG, "host")
+DRIVER = os.path.join(PKG, "lbmpsm_driver")
+
+
+def build_driver(force: bool = False) -> str:
+    """The C++ host side (host/lbmpsm_fix.cpp) and its standalone driver,
+    linked against liblbmpsm_gb300.so (found next to the binary at run time)."""
+    srcs = [os.path.join(HOST, f) for f in ("lbmpsm_fix.cpp", "lbmpsm_driver.cpp")]
+    deps = srcs + [os.path.join(HOST, "lbmpsm_fix.h"), os.path.join(ROOT, "include", "lbmpsm.h"), LIB]
+    if force or _stale(DRIVER, deps):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), "-I", HOST,
+               *srcs, "-o", DRIVER, "-L", PKG, "-llbmpsm_gb300", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host driver build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":
