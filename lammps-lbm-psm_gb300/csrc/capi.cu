@@ -76,6 +76,8 @@ struct lbmpsm_handle {
   // images, map + collide + reduce, download of the outputs and status word)
   cudaGraphExec_t hexec[2]{nullptr, nullptr};
   int hgraph_n = -1;
+  int hprev_n = -1;   // image count of the previous host-pointer step
+  int hsame = 0;      // consecutive host-pointer steps with that count
   PipeConfig pipe{};  // launch shape of the FP32/FP16 collide kernel
   float tune_ms[LBMPSM_TUNE_CANDIDATES] = {-1.f, -1.f, -1.f, -1.f};
   bool tune_pending = false;  // the collide autotuner has yet to run
@@ -996,8 +998,11 @@ int stage_images(lbmpsm_handle* h, int n, const int* box, const int* tag, const 
 // The device work of a step with images -- upload of the staged images, map,
 // collide, reduce, download of the outputs and of the status word -- is
 // captured once per A-A parity into a CUDA graph and replayed, so that a
-// step costs one graph launch and one synchronisation on the host.  Steps
-// that store the macroscopic fields run eagerly.
+// step costs one graph launch and one synchronisation on the host.  The
+// graphs are keyed by the image count, which changes whenever a ghost image
+// appears or goes: they are captured only once the count has held for two
+// calls in a row, and steps before that run eagerly, as do steps that store
+// the macroscopic fields.
 int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const double* x,
               const double* v, const double* omega, const double* radius, double* fh, double* th,
               double* stresslet) {
@@ -1026,7 +1031,9 @@ int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const dou
                                 h->stream));
     return LBMPSM_OK;
   };
-  if (h->macro_requested) {
+  h->hsame = n == h->hprev_n ? h->hsame + 1 : 0;
+  h->hprev_n = n;
+  if (h->macro_requested || (h->hgraph_n != n && h->hsame < 2)) {
     rc = enqueue_all();
     if (rc) return rc;
   } else {
