@@ -52,3 +52,18 @@ def test_no_cpu_fallback(has_gpu):
     with pytest.raises(lbmpsm.LbmPsmError) as e:
         lbmpsm.Lattice(prd=(8, 8, 8), Nlc=9, lc=8.0, nu=0.2 / 3, Re=1.0)
     assert e.value.code in (lbmpsm.ERR_CUDA, lbmpsm.ERR_NOMEM)
+
+
+def test_group_and_sensitivity_argument_checks_without_touching_the_gpu():
+    import ctypes as C
+    lib = lbmpsm.load()
+    g = C.c_void_p()
+    assert lib.lbmpsm_group_create(None, 0, C.byref(g)) == lbmpsm.ERR_ARG
+    assert b"at least one lattice" in lib.lbmpsm_last_error(None)
+    arr = (C.c_void_p * 2)(None, None)
+    assert lib.lbmpsm_group_create(arr, 2, C.byref(g)) == lbmpsm.ERR_ARG
+    assert lib.lbmpsm_group_run_fixed(None, 1) == lbmpsm.ERR_ARG
+    assert lib.lbmpsm_adjoint_drag(None, 0, None, None, None, None, None, 10, 1, 10, None, 5,
+                                   1e-4, None, None, None, None, None) == lbmpsm.ERR_ARG
+    assert lib.lbmpsm_tangent_drag(None, 0, None, None, None, None, None, 10, 1, 10, None, 1e-4,
+                                   0.0, None, None, None, None) == lbmpsm.ERR_ARG
