@@ -362,6 +362,31 @@ static __device__ __forceinline__ int classify_node(int hi, int hj, int hk, cons
   return -1;
 }
 
+// A shell node (between the early-out radii) whose sub-cells all lie on one
+// side of the surface: the count calcSolidFraction's loop would give
+// (src/LBM_PSM_exchangeParticleData.cpp:151-165), 10^dim or 0, else -1.
+// Every FP64 sub-cell sum (dx_sq[i] + dy_sq[j]) + dz_sq[k] is monotone in
+// each term and each term is convex in the sub-cell offset, so the largest
+// sum is the far corner's (|d| + 0.45 per axis) and the smallest is at least
+// the sum of max(|d| - 0.45, 0)^2.  Decided in FP32 with the margin M that
+// bounds the FP32 error of every sub-cell sum of the node (the one the shell
+// count uses); undecided nodes stay in the shell.
+static __device__ __forceinline__ int corner_count(int dim, float dxf, float dyf, float dzf,
+                                                   float rSqf) {
+  const float u = 5.9604644775390625e-08f;  // 2^-24
+  const float ax = fabsf(dxf), ay = fabsf(dyf), az = dim == 3 ? fabsf(dzf) : 0.0f;
+  const float Ea = ax + 2.0f, Eb = ay + 2.0f, Ec = az + 2.0f;
+  const float M = 16.0f * u * (Ea * Ea + Eb * Eb + (dim == 3 ? Ec * Ec : 0.0f) + rSqf);
+  const float fx = ax + 0.45f, fy = ay + 0.45f, fz = az + 0.45f;
+  const float far = fx * fx + fy * fy + (dim == 3 ? fz * fz : 0.0f);
+  if (far < rSqf - M) return dim == 3 ? 1000 : 100;
+  const float nx = fmaxf(ax - 0.45f, 0.0f), ny = fmaxf(ay - 0.45f, 0.0f),
+              nz = fmaxf(az - 0.45f, 0.0f);
+  const float near = nx * nx + ny * ny + (dim == 3 ? nz * nz : 0.0f);
+  if (near > rSqf + M) return 0;
+  return -1;
+}
+
 constexpr int SFC_THREADS = 256;  // classification: one block per image
 constexpr int SFS_THREADS = 128;  // shell counting: persistent warps
 constexpr int SFS_BUF = 352;      // per-warp buffer of crossing rows (>= 32 + 32*10)
@@ -372,9 +397,10 @@ static __device__ __forceinline__ float sub_offset(int k) {
 
 // Phase 1 of the map, one block per image: every node of the image box is
 // classified by the early-out radii of calcSolidFraction; inside / outside
-// nodes get their code here, shell nodes (whose sub-cells must be counted)
-// are queued in shared memory and appended to a global list with one atomic
-// per round of the block.
+// nodes get their code here, and so do shell nodes whose sub-cells all lie
+// on one side of the surface; the other shell nodes (whose sub-cells must be
+// counted) are queued in shared memory and appended to a global list with
+// one atomic per round of the block.
 constexpr int SFC_ROUND = 2048;
 __global__ void __launch_bounds__(SFC_THREADS) sf_classify_kernel(MapParams p) {
   const Img& im = p.img[blockIdx.x];
@@ -401,7 +427,8 @@ __global__ void __launch_bounds__(SFC_THREADS) sf_classify_kernel(MapParams p) {
       const int hy = im.lo[1] + q1 - q2 * wy + g.off[1];
       const int hz = im.lo[2] - im.zoff + q2 + g.off[2];  // z in the box's own frame
       float dxf, dyf, dzf;
-      const int c = classify_node(hx, hy, hz, im, dxf, dyf, dzf);
+      int c = classify_node(hx, hy, hz, im, dxf, dyf, dzf);
+      if (c < 0) c = corner_count(g.dim, dxf, dyf, dzf, im.rSqf);
       if (c >= 0) {
         code[li] = (unsigned short)c;
       } else {
@@ -1108,8 +1135,10 @@ static __device__ __forceinline__ void two_sum(float a, float b, float& s, float
 // forces carry FP32 precision), accumulated per particle in double-float
 // (hi + lo pairs combined with TwoSum, ~48-bit significand) on the FP32 pipe,
 // then the per-warp results summed in FP64.  (FP64 arithmetic runs at 1/64 of
-// the FP32 rate on this GPU.)
-__global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p) {
+// the FP32 rate on this GPU.)  Latency-bound: 64 registers (4 blocks per
+// multiprocessor) and two nodes' loads in flight per thread.
+constexpr int RED_U = 2;
+__global__ void __launch_bounds__(RED_THREADS, 4) reduce_f32_kernel(ReduceParams p) {
   const int ip = blockIdx.x;
   const Geom& g = p.g;
   const int tag = p.tag[ip];
@@ -1125,51 +1154,72 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f32_kernel(ReduceParams p)
     const float* nodeF = static_cast<const float*>(p.tab.nodeF);
     // x fastest: consecutive threads read consecutive nodes
     const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
-    for (int t = threadIdx.x; t < total; t += RED_THREADS) {
-      const int q1 = (int)fast_div((unsigned)t, fx);
-      const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int i = bx.qlo[0] + t - q1 * wx;
-      const int j = bx.qlo[1] + q1 - q2 * wy;
-      const int k = bx.qlo[2] + q2;
-      if (bx.solo && beyond_rP(bx, i, j, k)) continue;
-      const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2] + bx.zoff);
-      // both slots' forces are loaded with the ids (no second dependent load)
-      const int2 id = p.tab.ids[n];
-      const float2* nf2 = reinterpret_cast<const float2*>(nodeF + 6 * n);
-      const float2 f01 = nf2[0], f23 = nf2[1], f45 = nf2[2];
-      float F0, F1, F2;
-      if (tag == id.x) {
-        F0 = f01.x;
-        F1 = f01.y;
-        F2 = f23.x;
-      } else if (tag == id.y) {
-        F0 = f23.y;
-        F1 = f45.x;
-        F2 = f45.y;
-      } else {
-        continue;
-      }
-      const float dx = small_int_to_float(i - xi[0]) - xf[0];
-      const float dy = small_int_to_float(j - xi[1]) - xf[1];
-      const float dz = small_int_to_float(k - xi[2]) - xf[2];
-      const float term[12] = {F0,
-                              F1,
-                              F2,
-                              dy * F2 - dz * F1,
-                              dz * F0 - dx * F2,
-                              dx * F1 - dy * F0,
-                              dx * F0,
-                              dy * F1,
-                              dz * F2,
-                              0.5f * (dy * F0 + dx * F1),
-                              0.5f * (dz * F0 + dx * F2),
-                              0.5f * (dz * F1 + dy * F2)};
+    // RED_U nodes per iteration: their ids and forces are loaded before any
+    // is summed (more loads in flight per thread); each thread still sums
+    // its nodes t, t + RED_THREADS, ... in that order
+    for (int t0 = threadIdx.x; t0 < total; t0 += RED_U * RED_THREADS) {
+      int2 id[RED_U];
+      float2 f01[RED_U], f23[RED_U], f45[RED_U];
+      float dx[RED_U], dy[RED_U], dz[RED_U];
+      bool ok[RED_U];
 #pragma unroll
-      for (int q = 0; q < 12; ++q) {
-        float sv, e;
-        two_sum(hi[q], term[q], sv, e);
-        hi[q] = sv;
-        lo[q] += e;
+      for (int u = 0; u < RED_U; ++u) {
+        const int t = t0 + u * RED_THREADS;
+        const int q1 = (int)fast_div((unsigned)t, fx);
+        const int q2 = (int)fast_div((unsigned)q1, fy);
+        const int i = bx.qlo[0] + t - q1 * wx;
+        const int j = bx.qlo[1] + q1 - q2 * wy;
+        const int k = bx.qlo[2] + q2;
+        ok[u] = t < total && !(bx.solo && beyond_rP(bx, i, j, k));
+        id[u] = make_int2(0, 0);
+        f01[u] = f23[u] = f45[u] = make_float2(0.f, 0.f);
+        dx[u] = small_int_to_float(i - xi[0]) - xf[0];
+        dy[u] = small_int_to_float(j - xi[1]) - xf[1];
+        dz[u] = small_int_to_float(k - xi[2]) - xf[2];
+        if (ok[u]) {
+          const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2] + bx.zoff);
+          // both slots' forces are loaded with the ids (no second dependent load)
+          id[u] = p.tab.ids[n];
+          const float2* nf2 = reinterpret_cast<const float2*>(nodeF + 6 * n);
+          f01[u] = nf2[0];
+          f23[u] = nf2[1];
+          f45[u] = nf2[2];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < RED_U; ++u) {
+        if (!ok[u]) continue;
+        float F0, F1, F2;
+        if (tag == id[u].x) {
+          F0 = f01[u].x;
+          F1 = f01[u].y;
+          F2 = f23[u].x;
+        } else if (tag == id[u].y) {
+          F0 = f23[u].y;
+          F1 = f45[u].x;
+          F2 = f45[u].y;
+        } else {
+          continue;
+        }
+        const float term[12] = {F0,
+                                F1,
+                                F2,
+                                dy[u] * F2 - dz[u] * F1,
+                                dz[u] * F0 - dx[u] * F2,
+                                dx[u] * F1 - dy[u] * F0,
+                                dx[u] * F0,
+                                dy[u] * F1,
+                                dz[u] * F2,
+                                0.5f * (dy[u] * F0 + dx[u] * F1),
+                                0.5f * (dz[u] * F0 + dx[u] * F2),
+                                0.5f * (dz[u] * F1 + dy[u] * F2)};
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+          float sv, e;
+          two_sum(hi[q], term[q], sv, e);
+          hi[q] = sv;
+          lo[q] += e;
+        }
       }
     }
   }
