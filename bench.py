@@ -356,7 +356,7 @@ def run_ours(args, rank=0, world=1):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_steps)
+        out["cpu_baseline"] = cpu_baseline(args.cpu_steps, single_core=True)
     return out
 
 
@@ -369,9 +369,10 @@ def max_over_ranks(t, world):
     return float(v.item())
 
 
-def cpu_baseline(steps, threads=None):
+def cpu_baseline(steps, threads=None, single_core=False):
     """The CPU oracle (FP64, the reference's layout and arithmetic) on the same
-    workload, all host cores, a bounded number of coupling steps."""
+    workload, all host cores, a bounded number of coupling steps; with
+    single_core, also one step on one thread."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
@@ -387,13 +388,21 @@ def cpu_baseline(steps, threads=None):
     for _ in range(steps):
         sim.step(g.tag, g.x, g.v, g.omega, g.radius, bc=True)
     dt = time.perf_counter() - t0
-    sim.close()
     nodes = EDGE ** 3
-    return {"value": round(nodes * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": threads,
-            "kind": "port",
-            "sample": f"{steps} full coupling steps of the same 256^3 / 2000-sphere workload "
-                      f"(after 1 warm-up step), FP64, OpenMP over {threads} threads",
-            "seconds": round(dt, 2)}
+    out = {"value": round(nodes * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": threads,
+           "kind": "port",
+           "sample": f"{steps} full coupling steps of the same 256^3 / 2000-sphere workload "
+                     f"(after 1 warm-up step), FP64, OpenMP over {threads} threads",
+           "seconds": round(dt, 2)}
+    if single_core:
+        sim.set_threads(1)
+        t0 = time.perf_counter()
+        sim.step(g.tag, g.x, g.v, g.omega, g.radius, bc=True)
+        d1 = time.perf_counter() - t0
+        out["single_core"] = {"value": round(nodes / d1 / 1e6, 3), "unit": "MLUPS", "cores": 1,
+                              "sample": "1 full coupling step, one thread", "seconds": round(d1, 2)}
+    sim.close()
+    return out
 
 
 def run_reference(args, rank, world):
