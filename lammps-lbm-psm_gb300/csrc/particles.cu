@@ -515,17 +515,22 @@ static __device__ __noinline__ int exact_count_2d(const Img& im, int hx, int hy)
 //
 // 3-D: with the axes ordered so that the inner axis c has the smallest
 // |offset| (its rows run most nearly along the sphere surface, so fewest of
-// them cross it), each lane walks its node's 100 rows (a, b).  A row whose
-// 10 sub-cell sums are all below r^2 - M counts 10, one whose sums are all
-// above r^2 + M counts 0 (M bounds the FP32 error, 16x the worst case);
-// a row in between crosses the surface and is pushed into a per-warp buffer
-// that is drained 32 rows at a time, one row per lane: the count is the rank
-// of r^2 - M - s_ab among the node's 10 sorted c-terms, and a c-term within
-// the margin band makes the row ambiguous, in which case that row alone is
-// recounted exactly in FP64.
+// them cross it), a node's sub-cells are 10 slabs a of 100 rows (a, b).  A
+// row whose 10 sub-cell sums are all below r^2 - M counts 10, one whose sums
+// are all above r^2 + M counts 0 (M bounds the FP32 error, 16x the worst
+// case); a row in between crosses the surface.  Each lane first tests its
+// node's slabs as wholes: a slab whose largest row sum (its a-term plus the
+// largest b-term) passes the inside test counts 100, one whose smallest
+// fails the outside test counts 0 -- exactly what its rows would give, the
+// FP32 sums being monotone in each term.  The other slabs go to a per-warp
+// queue, taken one slab per lane: the slab's rows are tested and its
+// crossing rows pushed into a per-warp buffer that is drained 32 rows at a
+// time, one row per lane: the count is the rank of r^2 - M - s_ab among the
+// node's 10 sorted c-terms, and a c-term within the margin band makes the
+// row ambiguous, in which case that row alone is recounted exactly in FP64.
 // 2-D: 100 sub-cells per node, counted in FP32 with the same margin; a node
 // with any ambiguous sub-cell is recounted exactly.
-__global__ void __launch_bounds__(SFS_THREADS) sf_shell_kernel(MapParams p) {
+__global__ void __launch_bounds__(SFS_THREADS, 8) sf_shell_kernel(MapParams p) {
   constexpr int NW = SFS_THREADS / 32;
   __shared__ float s_sorted[NW][32][17];  // 10 sorted c-terms + padding (odd stride)
   __shared__ float s_lo[NW][32];
@@ -535,7 +540,9 @@ __global__ void __launch_bounds__(SFS_THREADS) sf_shell_kernel(MapParams p) {
   __shared__ int s_perm[NW][32];  // its axis order: pa | pb << 2
   __shared__ float s_dc[NW][32];  // its inner-axis offset
   __shared__ float buf_s[NW][SFS_BUF];
-  __shared__ int buf_o[NW][SFS_BUF];
+  __shared__ unsigned short buf_o[NW][SFS_BUF];   // owner lane | a << 5 | b << 9
+  __shared__ unsigned short q_slab[NW][32 * 10];  // partial slabs: owner lane | a << 5
+  __shared__ float s_da[NW][32], s_db[NW][32], s_lin[NW][32], s_hout[NW][32];
   const unsigned long long tot = p.pair_total[2];
   const int total = (int)min(tot, (unsigned long long)p.shell_cap);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -610,15 +617,50 @@ __global__ void __launch_bounds__(SFS_THREADS) sf_shell_kernel(MapParams p) {
       s_cnt[warp][lane] = 0;
       const float lo_in = lo - sc[9];   // row wholly inside: s_ab + max c-term < lo
       const float hi_out = hi - sc[0];  // row wholly outside: s_ab + min c-term > hi
-      float sb[10];
+      float sb_min = 3.0e38f, sb_max = 0.0f;
 #pragma unroll
       for (int b = 0; b < 10; ++b) {
         const float t = db + sub_offset(b);
-        sb[b] = t * t;
+        const float v = t * t;
+        sb_min = fminf(sb_min, v);
+        sb_max = fmaxf(sb_max, v);
       }
       s_ent[warp][lane] = valid ? e : base;
       s_perm[warp][lane] = pa | (pb << 2);
       s_dc[warp][lane] = dc;
+      s_da[warp][lane] = da;
+      s_db[warp][lane] = db;
+      s_lin[warp][lane] = lo_in;
+      s_hout[warp][lane] = hi_out;
+      // whole slabs: inside (100), outside (0), or partial (queued)
+      unsigned pm = 0;
+#pragma unroll
+      for (int a = 0; a < 10; ++a) {
+        const float ta = da + sub_offset(a);
+        const float sa = ta * ta;
+        const bool in = sa + sb_max < lo_in;
+        const bool out = sa + sb_min > hi_out;
+        n += in ? 100 : 0;
+        pm |= (!in && !out) ? (1u << a) : 0u;
+      }
+      if (!valid) pm = 0;
+      int nslab;
+      {
+        const int cnt = __popc(pm);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        int pos = incl - cnt;
+        while (pm) {
+          const int a = __ffs(pm) - 1;
+          pm &= pm - 1u;
+          q_slab[warp][pos++] = (unsigned short)(lane | (a << 5));
+        }
+        nslab = __shfl_sync(0xffffffffu, incl, 31);
+      }
       __syncwarp();
       // count of one buffered crossing row, added to its owner lane
       auto drain_row = [&](int k) {
@@ -642,18 +684,29 @@ __global__ void __launch_bounds__(SFS_THREADS) sf_shell_kernel(MapParams p) {
         if (rc) atomicAdd(&s_cnt[warp][ow], rc);
       };
       int wtotal = 0;  // rows in the warp buffer (warp-uniform)
-      for (int a = 0; a < 10; ++a) {
-        const float ta = da + sub_offset(a);
-        const float sa = ta * ta;
+      for (int k0 = 0; k0 < nslab; k0 += 32) {
+        // one partial slab per lane: its rows, the crossing ones buffered
         unsigned cm = 0;
+        int ow = 0, a = 0;
+        float sa = 0.0f;
+        if (k0 + lane < nslab) {
+          const int q = q_slab[warp][k0 + lane];
+          ow = q & 31;
+          a = q >> 5;
+          const float ta = s_da[warp][ow] + sub_offset(a);
+          sa = ta * ta;
+          const float dbo = s_db[warp][ow], lin = s_lin[warp][ow], hout = s_hout[warp][ow];
+          int in_rows = 0;
 #pragma unroll
-        for (int b = 0; b < 10; ++b) {
-          const float sv = sa + sb[b];
-          const bool inside = sv < lo_in;
-          n += inside ? 10 : 0;
-          cm |= (!inside && sv <= hi_out) ? (1u << b) : 0u;
+          for (int b = 0; b < 10; ++b) {
+            const float tb = dbo + sub_offset(b);
+            const float sv = sa + tb * tb;
+            const bool inside = sv < lin;
+            in_rows += inside ? 10 : 0;
+            cm |= (!inside && sv <= hout) ? (1u << b) : 0u;
+          }
+          if (in_rows) atomicAdd(&s_cnt[warp][ow], in_rows);
         }
-        if (!valid) cm = 0;
         // append the crossing rows to the warp buffer
         const int cnt = __popc(cm);
         int incl = cnt;
@@ -663,13 +716,16 @@ __global__ void __launch_bounds__(SFS_THREADS) sf_shell_kernel(MapParams p) {
           if (lane >= o) incl += t;
         }
         int pos = wtotal + incl - cnt;
-        while (cm) {
-          const int b = __ffs(cm) - 1;
-          cm &= cm - 1u;
-          const float tb = db + sub_offset(b);
-          buf_s[warp][pos] = sa + tb * tb;
-          buf_o[warp][pos] = lane | (a << 5) | (b << 9);
-          ++pos;
+        if (cm) {
+          const float dbo = s_db[warp][ow];
+          while (cm) {
+            const int b = __ffs(cm) - 1;
+            cm &= cm - 1u;
+            const float tb = dbo + sub_offset(b);
+            buf_s[warp][pos] = sa + tb * tb;
+            buf_o[warp][pos] = (unsigned short)(ow | (a << 5) | (b << 9));
+            ++pos;
+          }
         }
         wtotal += __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
