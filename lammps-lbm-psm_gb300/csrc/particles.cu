@@ -41,6 +41,7 @@ static __device__ __forceinline__ double local_centre(double x, double origin, d
 // (src/LBM_PSM_exchangeParticleData.cpp:188-195).
 static __device__ __forceinline__ void reduce_box_of(const Geom& g, const double xl[3], double r,
                                                      int lo[3], int hi[3]) {
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
     int a = (int)(xl[d] - r) - 2;
     int c = (int)(xl[d] + r) + 2;
@@ -66,10 +67,9 @@ static __device__ __forceinline__ void reduce_box_of(const Geom& g, const double
 }
 
 // One thread per image builds its record (the FP64 arithmetic of
-// src/LBM_PSM_exchangeParticleData.cpp:31-55); then the warp counts its 32
-// images into the cells their boxes touch, one image at a time with the
-// lanes spread over the image's cells, and reserves the images' ranges of
-// solid-fraction codes with one atomic per warp.
+// src/LBM_PSM_exchangeParticleData.cpp:31-55), counts the image into the
+// cells its box touches, and the warp reserves its images' ranges of
+// solid-fraction codes with one atomic.
 __global__ void img_prep_kernel(MapParams p) {
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -86,6 +86,7 @@ __global__ void img_prep_kernel(MapParams p) {
     const double r = p.radius[i] / p.dx;
     im.r = r;
     bool valid = true;
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
       const double xl = local_centre(p.x[3 * i + d], bp.origin[d], p.dx);
       im.xl[d] = xl;
@@ -124,6 +125,7 @@ __global__ void img_prep_kernel(MapParams p) {
     im.rP2f = (float)im.rP2;
     im.rM2f = (float)im.rM2;
     im.rSqf = (float)im.rSq;
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
       // xl = xi + xfrac exactly (the fractional part of a double is exact)
       const double xl = im.xl[d];
@@ -135,6 +137,7 @@ __global__ void img_prep_kernel(MapParams p) {
     // the node velocity reduces to uT + 0.0 bit for bit when every omega
     // component is +0.0 and no uT component is -0.0 (signed-zero arithmetic)
     bool plain = true;
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
       if (__double_as_longlong(im.om[d]) != 0ll) plain = false;
       if (__double_as_longlong(im.uT[d]) == (long long)0x8000000000000000ull) plain = false;
@@ -148,11 +151,14 @@ __global__ void img_prep_kernel(MapParams p) {
     // visits the box part around the sphere (and still checks each tag).
     {
       bool solo = true;
-      for (int d = 0; d < g.dim; ++d) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if (d >= g.dim) break;
         const int w = ((int)(im.xl[d] + r) + 2) - ((int)(im.xl[d] - r) - 2);
         if (g.per[d] && w >= (d == 2 ? g.bz : g.S[d])) solo = false;
       }
       im.solo = solo ? 1 : 0;
+#pragma unroll
       for (int d = 0; d < 3; ++d) {
         im.qlo[d] = im.rlo[d];
         im.qhi[d] = im.rhi[d];
@@ -163,9 +169,11 @@ __global__ void img_prep_kernel(MapParams p) {
         }
       }
     }
+#pragma unroll
     for (int d = 0; d < 3; ++d) im.box[d] = valid ? im.hi[d] - im.lo[d] : 0;
     if (valid) {
       vol = (unsigned long long)im.box[0] * im.box[1] * im.box[2];
+#pragma unroll
       for (int d = 0; d < 3; ++d) {
         im.clo[d] = im.lo[d] / p.cb[d];
         im.chi[d] = (im.hi[d] - 1) / p.cb[d];
@@ -173,6 +181,7 @@ __global__ void img_prep_kernel(MapParams p) {
         cr[3 + d] = im.chi[d];
       }
     } else {
+#pragma unroll
       for (int d = 0; d < 3; ++d) im.clo[d] = 0, im.chi[d] = -1;
     }
   }
@@ -201,21 +210,21 @@ __global__ void img_prep_kernel(MapParams p) {
     p.arec[3 * i + 2] = make_int4(__float_as_int(im.uTf[0]), __float_as_int(im.uTf[1]),
                                   __float_as_int(im.uTf[2]), 0);
   }
-  // cell counts, one image of the warp at a time
+  // cell counts: each lane walks the cells its image's box touches (integer
+  // sums, so the order of the atomics does not matter); one atomic per warp
+  // for the pair total
   unsigned long long pairs = 0;
-  for (int j = 0; j < 32; ++j) {
-    int c[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) c[k] = __shfl_sync(0xffffffffu, cr[k], j);
-    const int nx = c[3] - c[0] + 1, ny = c[4] - c[1] + 1, nz = c[5] - c[2] + 1;
-    if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
-    const int ncell = nx * ny * nz;
-    pairs += (unsigned long long)ncell;
-    for (int t = lane; t < ncell; t += 32) {
-      const int cx = c[0] + t % nx, cy = c[1] + (t / nx) % ny, cz = c[2] + t / (nx * ny);
-      atomicAdd(&p.cell_count[(cz * p.C[1] + cy) * p.C[0] + cx], 1);
-    }
+  if (cr[3] >= cr[0] && cr[4] >= cr[1] && cr[5] >= cr[2]) {
+    for (int cz = cr[2]; cz <= cr[5]; ++cz)
+      for (int cy = cr[1]; cy <= cr[4]; ++cy) {
+        int* row = p.cell_count + (cz * p.C[1] + cy) * p.C[0];
+        for (int cx = cr[0]; cx <= cr[3]; ++cx) atomicAdd(row + cx, 1);
+      }
+    pairs = (unsigned long long)(cr[3] - cr[0] + 1) * (unsigned long long)(cr[4] - cr[1] + 1) *
+            (unsigned long long)(cr[5] - cr[2] + 1);
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
   if (lane == 0 && pairs) atomicAdd(&p.pair_total[0], pairs);
 }
 
