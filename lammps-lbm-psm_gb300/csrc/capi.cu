@@ -39,6 +39,7 @@ struct lbmpsm_handle {
   cudaStream_t stream = nullptr;
   cudaStream_t aux = nullptr;                  // cell-list kernels of the map
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_bc_fork = nullptr, ev_bc_join = nullptr;  // the BC beside the reduction
   float scale16 = 4096.0f;
   // lattice
   void* f = nullptr;
@@ -453,7 +454,14 @@ int maybe_tune(lbmpsm_handle* h) {
 }
 
 // map -> collide -> reduce on device image arrays (internal buffers)
-int enqueue_step(lbmpsm_handle* h, int n) {
+int enqueue_bc(lbmpsm_handle* h, cudaStream_t st);
+
+// One coupling step (map, collide, reduce) on the handle's stream; with bc,
+// also the boundary faces after the collide.  The faces touch only the
+// populations, which neither the reduction nor the next step's map reads,
+// so with images the face kernel runs on the auxiliary stream beside the
+// reduction.
+int enqueue_step(lbmpsm_handle* h, int n, bool bc = false) {
   // image block layout: x | v | omega (3n each) | radius (n)
   const int* tag = h->d_tag;
   const double* x = h->d_xvw;
@@ -502,6 +510,20 @@ int enqueue_step(lbmpsm_handle* h, int n) {
   }
   int rc = collide(h);
   if (rc) return rc;
+  bool bc_aside = false;
+  if (bc && !h->faces.empty()) {
+    if (n > 0 && h->aux && h->ev_bc_fork && h->ev_bc_join) {
+      CUDA_TRY(h, cudaEventRecord(h->ev_bc_fork, h->stream));
+      CUDA_TRY(h, cudaStreamWaitEvent(h->aux, h->ev_bc_fork, 0));
+      rc = enqueue_bc(h, h->aux);
+      if (rc) return rc;
+      CUDA_TRY(h, cudaEventRecord(h->ev_bc_join, h->aux));
+      bc_aside = true;
+    } else {
+      rc = enqueue_bc(h, nullptr);
+      if (rc) return rc;
+    }
+  }
   if (n > 0) {
     ReduceParams rp{};
     rp.img = h->d_img;
@@ -516,12 +538,14 @@ int enqueue_step(lbmpsm_handle* h, int n) {
     rp.S = h->d_out + 6 * (size_t)n;
     CUDA_TRY(h, launch_reduce(rp, h->stream));
   }
+  if (bc_aside) CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->ev_bc_join, 0));
   h->last_n = n;
   return LBMPSM_OK;
 }
 
-int enqueue_bc(lbmpsm_handle* h) {
+int enqueue_bc(lbmpsm_handle* h, cudaStream_t st) {
   if (h->faces.empty()) return LBMPSM_OK;
+  if (!st) st = h->stream;
   BCParams b{};
   b.g = h->g;
   b.f = h->f;
@@ -531,9 +555,9 @@ int enqueue_bc(lbmpsm_handle* h) {
   b.scale16 = h->scale16;
   cudaError_t e;
   switch (h->opt.storage) {
-    case LBMPSM_STORAGE_FP64: e = launch_bc_f64(b, h->stream); break;
-    case LBMPSM_STORAGE_FP32: e = launch_bc_f32(b, h->stream); break;
-    default: e = launch_bc_f16(b, h->stream); break;
+    case LBMPSM_STORAGE_FP64: e = launch_bc_f64(b, st); break;
+    case LBMPSM_STORAGE_FP32: e = launch_bc_f32(b, st); break;
+    default: e = launch_bc_f16(b, st); break;
   }
   CUDA_TRY(h, e);
   return LBMPSM_OK;
@@ -749,7 +773,9 @@ int create_impl(int nbox, const lbmpsm_fix_params* ps, const lbmpsm_options* opt
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_bc_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_bc_join, cudaEventDisableTiming) != cudaSuccess)
     return bail(LBMPSM_ERR_CUDA);
   const size_t es = storage_bytes(o.storage);
   const size_t N = (size_t)g.N;
@@ -864,6 +890,8 @@ void lbmpsm_destroy(lbmpsm_handle* h) {
   if (h->aux) cudaStreamSynchronize(h->aux);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->ev_bc_fork) cudaEventDestroy(h->ev_bc_fork);
+  if (h->ev_bc_join) cudaEventDestroy(h->ev_bc_join);
   if (h->aux) cudaStreamDestroy(h->aux);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1121,7 +1149,7 @@ int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
 int lbmpsm_apply_bc(lbmpsm_handle* h) {
   if (!h) return LBMPSM_ERR_ARG;
   CUDA_TRY(h, cudaSetDevice(h->device));
-  return enqueue_bc(h);
+  return enqueue_bc(h, nullptr);
 }
 
 int lbmpsm_request_macro(lbmpsm_handle* h) {
@@ -1253,8 +1281,7 @@ int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps) {
   if (h->graph_n != n || h->graph_bc != use_bc || h->macro_requested) drop_run_graphs(h);
   // a requested macro store runs eagerly (it changes the kernel arguments)
   while (nsteps > 0 && h->macro_requested) {
-    int rc = enqueue_step(h, n);
-    if (!rc && use_bc) rc = enqueue_bc(h);
+    int rc = enqueue_step(h, n, use_bc);
     if (rc) return rc;
     --nsteps;
   }
@@ -1264,8 +1291,7 @@ int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps) {
       cudaGraph_t graph;
       CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
       const long long t0 = h->t;
-      int rc = enqueue_step(h, n);
-      if (!rc && use_bc) rc = enqueue_bc(h);
+      int rc = enqueue_step(h, n, use_bc);
       cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
       h->t = t0;  // captured, not run
       if (rc) return rc;
@@ -1869,8 +1895,7 @@ int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps) {
         lbmpsm_handle* h = g->hs[i];
         ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
         if (ce != cudaSuccess) break;
-        rc = enqueue_step(h, h->last_n);
-        if (!rc && !h->faces.empty()) rc = enqueue_bc(h);
+        rc = enqueue_step(h, h->last_n, true);
         if (rc) rc = gfail(g, rc, h->err);
         if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
         if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);

@@ -93,9 +93,10 @@ def test_ensemble_rejects_mixed_geometry_and_boundary_conditions():
 
 
 def test_group_of_ensembles_of_different_sizes_equals_separate_runs():
-    """Boxes of two sizes (an ensemble of 20^3 boxes, one of 16^3 boxes) and a
-    plain lattice stepped as one group -- one graph launch per step -- give the
-    same populations and forces as each advanced on its own."""
+    """Boxes of two sizes (an ensemble of 20^3 boxes, one of 16^3 boxes), a
+    plain lattice and a sheared lattice (Zou-He faces) stepped as one group --
+    one graph launch per step -- give the same populations and forces as each
+    advanced on its own."""
     def make(edge, seed):
         boxes = []
         for b, tau in enumerate((0.7, 0.85)):
@@ -130,6 +131,15 @@ def test_group_of_ensembles_of_different_sizes_equals_separate_runs():
         tag, x, v, w, r = cases.initial_particles(case)
         g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
         lat.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+        members.append(lat)
+        nimg.append(len(g["tag"]))
+        case = cases.CASES["shear_3d"]
+        lat = lbmpsm.Lattice(**case.params(), storage="fp32")
+        lat.set_bc(case.bc)
+        tag, x, v, w, r = cases.initial_particles(case)
+        g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
+        lat.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+        lat.apply_bc()
         members.append(lat)
         nimg.append(len(g["tag"]))
         return members, nimg
