@@ -1288,27 +1288,56 @@ __global__ void __launch_bounds__(RED_THREADS, 4) reduce_f32_kernel(ReduceParams
       }
     }
   }
-  // fixed-order double-float butterfly within the warp
+  // fixed-order double-float reduction within the warp: the first two levels
+  // halve the terms each lane carries (12 -> 6 -> 3, partners keeping
+  // complementary halves), the last three are a butterfly on three terms
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool up16 = (lane & 16) != 0, up8 = (lane & 8) != 0;
+  float h6[6], l6[6], h3[3], l3[3];
 #pragma unroll
-  for (int q = 0; q < 12; ++q) {
+  for (int k = 0; k < 6; ++k) {
+    const float sh = up16 ? hi[k] : hi[k + 6], sl = up16 ? lo[k] : lo[k + 6];
+    const float mh = up16 ? hi[k + 6] : hi[k], ml = up16 ? lo[k + 6] : lo[k];
+    const float rh = __shfl_xor_sync(0xffffffffu, sh, 16);
+    const float rl = __shfl_xor_sync(0xffffffffu, sl, 16);
+    float sv, e;
+    two_sum(mh, rh, sv, e);
+    h6[k] = sv;
+    l6[k] = ml + rl + e;
+  }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float h2 = __shfl_xor_sync(0xffffffffu, hi[q], o);
-      const float l2 = __shfl_xor_sync(0xffffffffu, lo[q], o);
+  for (int k = 0; k < 3; ++k) {
+    const float sh = up8 ? h6[k] : h6[k + 3], sl = up8 ? l6[k] : l6[k + 3];
+    const float mh = up8 ? h6[k + 3] : h6[k], ml = up8 ? l6[k + 3] : l6[k];
+    const float rh = __shfl_xor_sync(0xffffffffu, sh, 8);
+    const float rl = __shfl_xor_sync(0xffffffffu, sl, 8);
+    float sv, e;
+    two_sum(mh, rh, sv, e);
+    h3[k] = sv;
+    l3[k] = ml + rl + e;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, h3[k], o);
+      const float l2 = __shfl_xor_sync(0xffffffffu, l3[k], o);
       float sv, e;
-      two_sum(hi[q], h2, sv, e);
-      hi[q] = sv;
-      lo[q] = lo[q] + l2 + e;
+      two_sum(h3[k], h2, sv, e);
+      h3[k] = sv;
+      l3[k] = l3[k] + l2 + e;
     }
   }
   // warps in index order, still in double-float; one FP64 sum per term
   __shared__ float part_hi[RED_THREADS / 32][12], part_lo[RED_THREADS / 32][12];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0)
-    for (int q = 0; q < 12; ++q) {
-      part_hi[warp][q] = hi[q];
-      part_lo[warp][q] = lo[q];
+  if ((lane & 7) == 0) {  // lanes 0, 8, 16, 24 hold terms 0-2, 3-5, 6-8, 9-11
+    const int q0 = (up16 ? 6 : 0) + (up8 ? 3 : 0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      part_hi[warp][q0 + k] = h3[k];
+      part_lo[warp][q0 + k] = l3[k];
     }
+  }
   __syncthreads();
   if (threadIdx.x < 12) {
     const int q = threadIdx.x;
