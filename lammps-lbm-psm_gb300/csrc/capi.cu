@@ -59,6 +59,7 @@ struct lbmpsm_handle {
   int4* d_arec = nullptr;   // compact image records of the table update (3 per image)
   int* d_cells = nullptr;   // count | off | fill (3*ncells)
   int* d_list = nullptr;
+  int4* d_lrec = nullptr;  // records per cell-list entry (3 int4 each)
   unsigned short* d_sfcode = nullptr;  // solid-fraction codes of (image, box node) pairs
   long long sf_cap = 0;
   unsigned long long* d_pair_total = nullptr;  // [0] list pairs, [1] codes, [2] shell nodes
@@ -250,6 +251,8 @@ void free_particles(lbmpsm_handle* h) {
   dfree(h->d_img_box);
   h->d_img_box = nullptr;
   dfree(h->d_list);
+  dfree(h->d_lrec);
+  h->d_lrec = nullptr;
   dfree(h->d_sfcode);
   dfree(h->d_shell);
   h->d_sfcode = nullptr;
@@ -324,9 +327,12 @@ int ensure_particles(lbmpsm_handle* h, int n, double max_r_phys) {
   if (need > h->list_cap) {
     drop_graphs(h);
     dfree(h->d_list);
+    dfree(h->d_lrec);
     h->d_list = nullptr;
+    h->d_lrec = nullptr;
     long long cap = std::max(need, 2 * h->list_cap);
     CUDA_TRY(h, dmalloc(h, &h->d_list, sizeof(int) * (size_t)cap));
+    CUDA_TRY(h, dmalloc(h, &h->d_lrec, sizeof(int4) * 3 * (size_t)cap));
     h->list_cap = cap;
   }
   // solid-fraction codes: one per node of every image box, box edge <= 2r+6
@@ -495,6 +501,7 @@ int enqueue_step(lbmpsm_handle* h, int n, bool bc = false) {
     m.cell_off = h->d_cells + ncells;
     m.cell_fill = h->d_cells + 2 * (size_t)ncells;
     m.list = h->d_list;
+    m.lrec = h->d_lrec;
     m.list_cap = h->list_cap;
     m.pair_total = h->d_pair_total;
     m.sfcode = h->d_sfcode;

@@ -302,6 +302,8 @@ struct MapParams {
   int* cell_off;
   int* cell_fill;
   int* list;
+  int4* lrec;         // per cell-list entry: its image's three records above (the
+                      // third with the image index in w), written by cell_sort
   long long list_cap;
   unsigned long long* pair_total;  // [0] cell-list pairs, [1] solid-fraction codes, [2] shell nodes
   unsigned short* sfcode;          // codes of all (image, box node) pairs

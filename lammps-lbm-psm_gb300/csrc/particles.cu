@@ -326,7 +326,8 @@ __global__ void cell_sort_kernel(MapParams p, int ncells) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   if (p.pair_total[0] > (unsigned long long)p.list_cap) return;
-  int* a = p.list + p.cell_off[c];
+  const int off = p.cell_off[c];
+  int* a = p.list + off;
   const int m = p.cell_count[c];
   for (int k = 1; k < m; ++k) {
     const int v = a[k];
@@ -337,6 +338,16 @@ __global__ void cell_sort_kernel(MapParams p, int ncells) {
     }
     a[j + 1] = v;
   }
+  // the images' table-update records in list order (FP32 / FP16 storage)
+  if (p.write32)
+    for (int k = 0; k < m; ++k) {
+      const int ii = a[k];
+      int4* r = p.lrec + 3 * ((long long)off + k);
+      r[0] = p.arec[3 * ii];
+      r[1] = p.arec[3 * ii + 1];
+      const int4 u = p.arec[3 * ii + 2];
+      r[2] = make_int4(u.x, u.y, u.z, ii);
+    }
 }
 
 // Early-out part of calcSolidFraction for one node, decided in FP32 with a
@@ -968,10 +979,12 @@ static __device__ __forceinline__ float4 spin_velocity(const Img& im, int hi, in
 
 // NPT nodes per thread (z, z + blockDim.z, ... within the cell; one node in
 // 2-D) of a cell that some image box touches.  The images of the cell's list
-// are visited in image order through their compact records (three 16-byte
-// loads instead of the scattered fields of Img), each record serving all the
-// thread's nodes, whose code, slot id and slot record loads are independent;
-// the slot ids are loaded on first use only.
+// are visited in image order through their compact records, which cell_sort
+// copied next to the list entries (three 16-byte loads straight after the
+// cell's offset, instead of list index, then record, then the scattered
+// fields of Img), each record serving all the thread's nodes, whose code,
+// slot id and slot record loads are independent; the slot ids are loaded on
+// first use only.
 template <int NPT>
 __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p) {
   const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
@@ -992,14 +1005,13 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
 #pragma unroll
   for (int k = 0; k < NPT; ++k)
     has[k] = (int)threadIdx.z + k * dz < p.cb[2] && sz0 + k * dz < g.S[2];
-  const int* lst = p.list + p.cell_off[c];
+  const int4* lrec = p.lrec + 3 * (long long)p.cell_off[c];
   Apply32 st[NPT];
   bool have[NPT];
 #pragma unroll
   for (int k = 0; k < NPT; ++k) have[k] = false;
   for (int t = 0; t < cnt; ++t) {
-    const int ii = lst[t];
-    const int4 A = p.arec[3 * ii];
+    const int4 A = lrec[3 * t];
     const unsigned ax = (unsigned)A.x, ay = (unsigned)A.y, az = (unsigned)A.z;
     const int lo0 = (int)(ax & 0xFFFFu), lo1 = (int)(ay & 0xFFFFu), lo2 = (int)(az & 0xFFFFu);
     const int hi2 = (int)(az >> 16);
@@ -1013,7 +1025,7 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
       any = any || in[k];
     }
     if (!any) continue;
-    const int4 B = p.arec[3 * ii + 1];
+    const int4 B = lrec[3 * t + 1];
     const unsigned bz = (unsigned)B.z;
     const int bx = (int)(bz & 0xFFFFu), by = (int)(bz >> 16);
     const long long off = (long long)(((unsigned long long)(unsigned)B.y << 32) |
@@ -1037,10 +1049,10 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
         if (!in[k]) continue;
         const int z = sz0 + k * dz;
         const int hk = z - box_of_z(g, z) * g.bz + g.off[2];  // z in the box's own frame
-        st[k].image(p, n0 + k * zstride, A.w, cd[k], spin_velocity(p.img[ii], hi, hj, hk));
+        st[k].image(p, n0 + k * zstride, A.w, cd[k], spin_velocity(p.img[lrec[3 * t + 2].w], hi, hj, hk));
       }
     } else {
-      const int4 U = p.arec[3 * ii + 2];
+      const int4 U = lrec[3 * t + 2];
       const float4 nv = make_float4(0.f, __int_as_float(U.x), __int_as_float(U.y),
                                     __int_as_float(U.z));
 #pragma unroll
