@@ -259,7 +259,13 @@ def run_ours(args, rank=0, world=1):
                                                  [round(float(t), 4) for t in info.collide_tune_ms]))}
     acc32 = accuracy_point(lat)
 
-    # end to end: host arrays through lbmpsm_step, copies every step
+    # end to end: host arrays through lbmpsm_step, copies every step; W
+    # untimed steps first (the library captures its host-step graph once the
+    # image count has held for two calls)
+    for _ in range(max(W, 3)):
+        lat.step(g.tag, g.x, g.v, g.omega, g.radius)
+        lat.apply_bc()
+    lat.synchronize()
     t0 = time.perf_counter()
     for _ in range(K):
         lat.step(g.tag, g.x, g.v, g.omega, g.radius)
