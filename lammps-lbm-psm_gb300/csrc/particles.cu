@@ -905,9 +905,10 @@ __global__ void __launch_bounds__(512) node_apply_kernel(MapParams p) {
 // images the node velocity is formed in FP32).
 //
 // One node's update state: the tags of its two slots as they stand after
-// the images applied so far.  Slot records are compared with the table and
-// written through when they change, so only the ids live in registers; the
-// ids and the flag are written back at the end if they changed.
+// the images applied so far.  Slot records are written through (the table
+// ends with the same records as when only changed ones are written, without
+// a read before the write), so only the ids live in registers; the ids and
+// the flag are written back at the end if they changed.
 struct Apply32 {
   int id0, id1;
   bool ids_dirty;
@@ -943,18 +944,12 @@ struct Apply32 {
     if (slot < 0) return;
     nv.x = cd == SF_ONE ? 1.0f : p.sf_value32[cd];
     const int cur = slot == 0 ? id0 : id1;
-    // re-setting a slot to the values it already holds changes nothing
-    if (cur == tag) {
-      const float4 r = p.tab.rec32[2 * n + slot];
-      if (__float_as_int(r.x) == __float_as_int(nv.x) &&
-          __float_as_int(r.y) == __float_as_int(nv.y) &&
-          __float_as_int(r.z) == __float_as_int(nv.z) &&
-          __float_as_int(r.w) == __float_as_int(nv.w))
-        return;
-    } else {
+    if (cur != tag) {
       if (slot == 0) id0 = tag; else id1 = tag;
       ids_dirty = true;
     }
+    // written whether or not it changes: a store does not wait, whereas
+    // reading the record first to skip an unchanged one would
     p.tab.rec32[2 * n + slot] = nv;
   }
 
