@@ -55,6 +55,16 @@ def test_corner_rule_agrees_with_the_reference_count():
             node[2] = 0
             xl[2] = 0.0
         dx, dy, dz = node - xl
+        if trial % 2:
+            # the node's farthest or nearest sub-cell centre a hair from the
+            # surface: only the margin keeps the FP32 rule from deciding it
+            sums = [(dx + DELTA) ** 2, (dy + DELTA) ** 2,
+                    (dz + DELTA) ** 2 if dim == 3 else np.zeros(1)]
+            pick = max if trial % 4 == 1 else min
+            s2 = pick(sums[0]) + pick(sums[1]) + pick(sums[2])
+            r = float(np.sqrt(s2)) * (1.0 + 1e-12 * rng.integers(-1, 2))
+            if r < 0.3:
+                continue
         dist = dx * dx + dy * dy + dz * dz
         rp, rm = r + half[dim], r - half[dim]
         if dist > rp * rp or dist < rm * rm:
