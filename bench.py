@@ -99,6 +99,38 @@ def images(edge=None, nspheres=None):
     return ghost_images(dom, DIAM / 2 + 3.0, np.arange(1, n + 1), x, np.zeros((n, 3)), np.zeros((n, 3)), r), n
 
 
+MOVE_SETS = 32      # the images' positions repeat after this many steps
+MOVE_AMP = 0.1      # lattice units: each sphere walks a closed loop of this radius
+MOVE_SEED = 20261205
+
+
+def moving_image_sets(g, nloc, nsets=MOVE_SETS, amp=MOVE_AMP, seed=MOVE_SEED):
+    """Positions and velocities of the images for nsets consecutive steps: every
+    sphere moves on its own seeded closed loop (an ellipse of radius `amp`
+    lattice units in a random plane, one turn per nsets steps, top speed
+    2*pi*amp/nsets ~ 0.02 lattice units per step), its ghost images with it,
+    so that the map sees new sub-cell positions on every step.  Returns
+    x[nsets, n, 3] and v[nsets, n, 3] (v = displacement per step)."""
+    rng = np.random.default_rng(seed)
+    n = len(g.tag)
+    a = rng.normal(size=(nloc, 3))
+    b = rng.normal(size=(nloc, 3))
+    a /= np.linalg.norm(a, axis=1, keepdims=True)
+    b -= a * np.einsum("ij,ij->i", a, b)[:, None]
+    b /= np.linalg.norm(b, axis=1, keepdims=True)
+    phase = rng.uniform(0.0, 2 * np.pi, nloc)
+    # the local atom each image was copied from (ghosts of ghosts resolved)
+    src = np.asarray(g.owner).copy()
+    for _ in range(4):
+        src = np.where(src >= nloc, np.asarray(g.owner)[src], src)
+    t = 2 * np.pi * np.arange(nsets + 1)[:, None] / nsets + phase[None, :]
+    d = amp * (np.cos(t)[..., None] * a[None] + np.sin(t)[..., None] * b[None])  # (nsets+1, nloc, 3)
+    d -= d[0][None]  # the first set is the RSA placement itself
+    x = np.asarray(g.x)[None] + d[:nsets, src]
+    v = (d[1:] - d[:-1])[:, src]
+    return np.ascontiguousarray(x), np.ascontiguousarray(v)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 50 ms; only the
     samples that arrive inside the marked timed window are summarised."""
@@ -189,6 +221,43 @@ def profile_traffic():
     return None
 
 
+class MovingImages:
+    """The images of the suspension workload on the device, one position and
+    velocity set per step of the closed loops (moving_image_sets), uploaded
+    once; step k hands set k % MOVE_SETS to lbmpsm_step_device, so that every
+    step maps images that have moved."""
+
+    def __init__(self, g, nloc, device):
+        import torch
+        xs, vs = moving_image_sets(g, nloc)
+        self.n = len(g.tag)
+        self.nsets = len(xs)
+        dev = torch.device("cuda", device)
+        self.tag = torch.as_tensor(np.asarray(g.tag, np.int32), device=dev)
+        self.x = torch.as_tensor(xs, device=dev)
+        self.v = torch.as_tensor(vs, device=dev)
+        self.omega = torch.zeros((self.n, 3), dtype=torch.float64, device=dev)
+        self.radius = torch.as_tensor(np.asarray(g.radius, np.float64), device=dev)
+        self.host = (np.asarray(g.tag, np.int32), xs, vs, np.zeros((self.n, 3)),
+                     np.asarray(g.radius, np.float64))
+        torch.cuda.synchronize(dev)
+
+    def step(self, lat, k, bc=True):
+        j = k % self.nsets
+        lat.step_device(self.n, self.tag.data_ptr(), self.x[j].data_ptr(), self.v[j].data_ptr(),
+                        self.omega.data_ptr(), self.radius.data_ptr())
+        if bc:
+            lat.apply_bc()
+
+    def host_step(self, lat, k):
+        """The same step through the host-pointer call (pinned copies inside)."""
+        t, xs, vs, w, r = self.host
+        j = k % self.nsets
+        out = lat.step(t, xs[j], vs[j], w, r)
+        lat.apply_bc()
+        return out
+
+
 def run_ours(args, rank=0, world=1):
     import torch
 
@@ -201,10 +270,11 @@ def run_ours(args, rank=0, world=1):
     n = len(g.tag)
     prm = workload_params(edge)
     nodes = edge * edge * edge
+    mov = MovingImages(g, nloc, device)
 
     def make(storage):
         lat = lbmpsm.Lattice(**prm, storage=storage, device=device, max_images=n,
-                             max_radius=DIAM / 2)
+                             max_radius=DIAM / 2 + MOVE_AMP)
         lat.set_bc("shear")
         return lat
 
@@ -221,55 +291,43 @@ def run_ours(args, rank=0, world=1):
         return e0.elapsed_time(e1) / 1e3
 
     K, W = args.steps, args.warmup
-    from lbmpsm.host import reverse_comm
 
-    def owner_forces(lt):
-        """F, T, S of the local particles after the ghost images' partial
-        sums are added into their owners (CommBrick::reverse_comm)."""
-        parts = lt.read_forces(n)
-        return [reverse_comm(a, g.owner, g.swap, nloc)[:nloc] for a in parts]
+    def moving(lt, k0, steps):
+        def go():
+            for k in range(k0, k0 + steps):
+                mov.step(lt, k)
+        return go
 
-    def accuracy_point(lt):
-        """One more host step with the macro fields requested: forces and the
-        velocity field after 2 + W + K steps."""
-        lt.request_macro()
-        lt.step(g.tag, g.x, g.v, g.omega, g.radius)
-        lt.apply_bc()
-        fts = owner_forces(lt)
-        u = lt.export_fields(1.0, 1.0, 1.0, as_double=True)[2]
-        return fts, u, lt.check()[0]
-
-    # FP32 storage: the headline path
+    # FP32 storage: the headline path.  The first step goes through the host
+    # call (images up, map, autotuner pending); then W untimed and K timed
+    # device steps, the images moving every step
     lat = make(args.storage)
-    mass0 = lat.check()[0]
-    lat.step(g.tag, g.x, g.v, g.omega, g.radius)  # images go up once, map + step
-    lat.apply_bc()
+    mov.host_step(lat, 0)
     with ClockSampler(device) as clk:
-        lat.run_fixed(W)
+        moving(lat, 1, W)()
         lat.synchronize()
         if world > 1:
             torch.distributed.barrier()
         t_a = time.monotonic()
-        t_val = ev_time(lat, lambda: lat.run_fixed(K))
+        t_val = ev_time(lat, moving(lat, 1 + W, K))
         clk.mark(t_a, time.monotonic())
     t_val = max_over_ranks(t_val, world)
     info = lat.get_info()  # the collide autotuner ran at the second step
     launch = {"stages": int(info.collide_stages), "blocks": int(info.collide_blocks),
               "tuner_ms_per_step_pair": dict(zip(["3", "2", "4", "5"],
                                                  [round(float(t), 4) for t in info.collide_tune_ms]))}
-    acc32 = accuracy_point(lat)
 
     # end to end: host arrays through lbmpsm_step, copies every step; W
     # untimed steps first (the library captures its host-step graph once the
     # image count has held for two calls)
-    for _ in range(max(W, 3)):
-        lat.step(g.tag, g.x, g.v, g.omega, g.radius)
-        lat.apply_bc()
+    k0 = 1 + W + K
+    for k in range(k0, k0 + max(W, 3)):
+        mov.host_step(lat, k)
     lat.synchronize()
+    k0 += max(W, 3)
     t0 = time.perf_counter()
-    for _ in range(K):
-        lat.step(g.tag, g.x, g.v, g.omega, g.radius)
-        lat.apply_bc()
+    for k in range(k0, k0 + K):
+        mov.host_step(lat, k)
     lat.synchronize()
     t_e2e = max_over_ranks(time.perf_counter() - t0, world)
 
@@ -283,37 +341,21 @@ def run_ours(args, rank=0, world=1):
     t_kernel = ev_time(lat, lattice_only(lat, K)) / K
     lat.close()
 
-    # plain FP64 path on the same workload, same step count at the accuracy point
+    # plain FP64 path on the same moving workload
     fp64 = None
-    accuracy = None
     if not args.no_fp64:
         lat64 = make("fp64")
-        lat64.step(g.tag, g.x, g.v, g.omega, g.radius)
-        lat64.apply_bc()
+        mov.host_step(lat64, 0)
         K64 = max(3, K // 8)
-        lat64.run_fixed(max(0, W + K - K64))
-        lat64.synchronize()
-        t64 = ev_time(lat64, lambda: lat64.run_fixed(K64))
-        acc64 = accuracy_point(lat64)
+        moving(lat64, 1, 2)()
+        t64 = ev_time(lat64, moving(lat64, 3, K64))
         t64_kernel = ev_time(lat64, lattice_only(lat64, 3)) / 3
         lat64.close()
-        mlups64 = nodes * K64 / t64 / 1e6
-        fp64 = (mlups64, t64_kernel)
+        fp64 = (nodes * K64 / t64 / 1e6, t64_kernel)
 
-        def rel(a, b):
-            return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
-        (F32, T32, S32), u32, m32 = acc32
-        (F64, T64, S64), u64, m64 = acc64
-        accuracy = {
-            "vs": "FP64 GPU path (bit-identical to the CPU oracle on the parity cases)",
-            "step": 2 + W + K,
-            "drag": rel(F32, F64), "torque": rel(T32, T64), "stresslet": rel(S32, S64),
-            "velocity_l2": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
-            "velocity_max": rel(u32, u64),
-            "mass_drift_fp32": float((m32 - mass0) / mass0),
-            "mass_drift_fp64": float((m64 - mass0) / mass0),
-            "metric": "max |x32 - x64| / max |x64| over particles (F, T, S) or nodes (u)",
-        }
+    accuracy = None
+    if not args.no_accuracy and not args.no_fp64:
+        accuracy = developed_accuracy(args, make, mov, nloc, g)
 
     mlups = whole_job_mlups(nodes, K, world, t_val)
     peak, peak_kind = measured_peak_gbs()
@@ -336,8 +378,12 @@ def run_ours(args, rank=0, world=1):
         "data": "synthetic",
         "config": {
             "workload": f"sheared suspension: D3Q19 {edge}^3, y Zou-He shear walls +-0.01, tau 0.65, "
-                        f"{nloc} spheres D=12 (seeded RSA), {args.storage.upper()} storage, FP64 F/T/S",
+                        f"{nloc} spheres D=12 (seeded RSA) moving on seeded closed loops (new "
+                        f"positions every step), {args.storage.upper()} storage, FP64 F/T/S",
             "nodes": nodes, "particles": nloc, "images": n, "storage": args.storage,
+            "motion": f"every sphere on its own closed loop of radius {MOVE_AMP} lattice units, "
+                      f"period {MOVE_SETS} steps (top speed ~0.02 lattice units per step); "
+                      "positions uploaded once, handed to lbmpsm_step_device each step",
             "l2": "lattice 1.27 GB > 129 MB L2: no flush needed",
             "parallelism": f"replicas x{world}",
         },
@@ -350,12 +396,13 @@ def run_ours(args, rank=0, world=1):
                                "(warp-specialised row pipeline, A-A even/odd)",
                      "algorithmic_bytes_per_node": BYTES_PER_NODE[args.storage],
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "step_hbm_frac": round(BYTES_PER_NODE[args.storage] * nodes / (t_val / K) / 1e9 / peak, 4),
         "fp64_plain": None if fp64 is None else {
             "value": round(fp64[0], 1), "unit": "MLUPS", "kernel_ms": round(fp64[1] * 1e3, 3),
             "hbm_frac": round(BYTES_PER_NODE["fp64"] * nodes / fp64[1] / 1e9 / peak, 4)},
         "fp32_over_fp64": None if fp64 is None else round(mlups / world / fp64[0], 2),
-        "drag_rel_err_fp32_vs_fp64": None if accuracy is None else accuracy["drag"],
-        "accuracy_fp32_vs_fp64": accuracy,
+        "drag_rel_err_fp32_vs_fp64": None if accuracy is None else accuracy["suspension"]["fp32"]["drag"],
+        "accuracy_vs_fp64": accuracy,
         "kernel_ms": round(t_kernel * 1e3, 4),
         "collide_launch": launch,
         "gpu_launches": launches_per_step * K,
@@ -364,6 +411,83 @@ def run_ours(args, rank=0, world=1):
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_steps, single_core=True)
     return out
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def developed_accuracy(args, make, mov, nloc, g):
+    """FP32 (and FP16, BF16) storage against the plain FP64 path at developed
+    states, every run from rest with the same inputs:
+      * the suspension itself after args.acc_steps coupling steps (default
+        2000, about 0.7 viscous times D^2/nu of a sphere) with the images
+        moving every step: drag, torque and stresslet of the 2000 spheres
+        (ghost rows summed into their owners), velocity field, mass drift;
+      * the single-sphere configuration (D3Q19 128^3 periodic, tau 0.7,
+        Fext (1e-6, 0, 0), sphere of diameter 16 at the centre) after
+        args.acc_c2_steps steps (default 10^4): drag and velocity field.
+    Errors: max |x - x64| / max |x64| over particles (F, T, S) or nodes (u),
+    and the L2 norm ratio for u."""
+    import lbmpsm
+    from lbmpsm.host import reverse_comm
+
+    storages = ["fp32", "fp16"] + (["bf16"] if "bf16" in lbmpsm.STORAGE else [])
+    res = {}
+
+    def susp(storage):
+        lt = make(storage)
+        mass0 = lt.check()[0]
+        mov.host_step(lt, 0)
+        for k in range(1, args.acc_steps - 1):
+            mov.step(lt, k)
+        lt.request_macro()
+        mov.host_step(lt, args.acc_steps - 1)
+        parts = lt.read_forces(len(g.tag))
+        fts = [reverse_comm(a, g.owner, g.swap, nloc)[:nloc] for a in parts]
+        u = lt.export_fields(1.0, 1.0, 1.0, as_double=True)[2]
+        m = lt.check()[0]
+        lt.close()
+        return fts, u, (m - mass0) / mass0
+
+    (F64, T64, S64), u64, d64 = susp("fp64")
+    block = {"steps": args.acc_steps, "mass_drift_fp64": float(d64)}
+    for st in storages:
+        (F, T, S), u, d = susp(st)
+        block[st] = {"drag": _rel(F, F64), "torque": _rel(T, T64), "stresslet": _rel(S, S64),
+                     "velocity_l2": float(np.linalg.norm(u - u64) / np.linalg.norm(u64)),
+                     "velocity_max": _rel(u, u64), "mass_drift": float(d)}
+    res["suspension"] = block
+
+    # the single-sphere configuration at 10^4 steps
+    nu = (0.7 - 0.5) / 3.0
+    c2 = dict(dimension=3, boxlo=(0.0, 0.0, 0.0), prd=(128.0,) * 3, periodic=(1, 1, 1), nevery=1,
+              Nlc=17, lc=16.0, rho=1.0, nu=nu, Re=0.01 * 16 / nu, tau=0.7, Fext=(1e-6, 0.0, 0.0))
+    one = [np.array([1], np.int32), np.array([[64.0, 64.0, 64.0]]), np.zeros((1, 3)),
+           np.zeros((1, 3)), np.array([8.0])]
+
+    def sphere(storage):
+        lt = lbmpsm.Lattice(**c2, storage=storage)
+        lt.step(*one)
+        lt.run_fixed(args.acc_c2_steps - 2)
+        lt.request_macro()
+        fh = lt.step(*one)[0]
+        u = lt.export_fields(1.0, 1.0, 1.0, as_double=True)[2]
+        lt.close()
+        return fh, u
+
+    F64, u64 = sphere("fp64")
+    block = {"steps": args.acc_c2_steps, "config": "D3Q19 128^3 periodic, tau 0.7, Fext (1e-6,0,0), "
+             "one fixed sphere D=16 at the centre", "drag_fp64": float(F64[0, 0])}
+    for st in storages:
+        F, u = sphere(st)
+        block[st] = {"drag": float(abs(F[0, 0] - F64[0, 0]) / abs(F64[0, 0])),
+                     "velocity_l2": float(np.linalg.norm(u - u64) / np.linalg.norm(u64)),
+                     "velocity_max": _rel(u, u64)}
+    res["single_sphere"] = block
+    res["vs"] = ("the plain FP64 GPU path (bit-identical to the CPU oracle's table and within "
+                 "1e-12 of its forces on the parity cases and on this workload's first steps)")
+    return res
 
 
 def max_over_ranks(t, world):
@@ -721,6 +845,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the developed-flow accuracy runs against FP64")
+    ap.add_argument("--acc-c2-steps", type=int, default=10000,
+                    help="steps of the single-sphere accuracy run")
     ap.add_argument("--edge", type=int, default=EDGE, help="lattice edge (profiling cases)")
     ap.add_argument("--nspheres", type=int, default=NSPHERES)
     ap.add_argument("--storage", choices=["fp32", "fp16"], default="fp32")
@@ -729,7 +857,8 @@ def main():
                          "adjoint: the drag-sensitivity sweep")
     ap.add_argument("--boxes", type=int, default=ENS_BOXES)
     ap.add_argument("--acc-boxes", type=int, default=8, help="ensemble: boxes per class compared with FP64")
-    ap.add_argument("--acc-steps", type=int, default=2000)
+    ap.add_argument("--acc-steps", type=int, default=2000,
+                    help="steps of the accuracy runs (suspension; ensemble boxes)")
     ap.add_argument("--adj-edge", type=int, default=ADJ_EDGE, help="adjoint: lattice edge")
     ap.add_argument("--adj-steps", type=int, default=ADJ_T, help="adjoint: steps (window: 2nd half)")
     ap.add_argument("--adj-checkpoint", type=int, default=ADJ_K)

@@ -43,7 +43,9 @@ extern "C" {
 #define LBMPSM_ERR_NOMEM (-4)    /* device or pinned host allocation failed */
 #define LBMPSM_ERR_CUDA (-5)     /* a CUDA runtime call failed */
 #define LBMPSM_ERR_STATE (-6)    /* call not valid in the handle's current state */
-#define LBMPSM_ERR_CAPACITY (-7) /* more particle images than the handle was sized for */
+#define LBMPSM_ERR_CAPACITY (-7) /* more particle images than the handle was sized for, or a
+                                   lbmpsm_export_fields_static request beyond
+                                   LBMPSM_EXPORT_STATIC_MAX_BYTES */
 #define LBMPSM_ERR_NUMERIC (-8)  /* non-finite populations or mass drift detected */
 #define LBMPSM_ERR_TIMEOUT (-9)  /* a bounded device-side wait gave up */
 

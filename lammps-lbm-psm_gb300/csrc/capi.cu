@@ -81,6 +81,7 @@ struct lbmpsm_handle {
   int hprev_n = -1;   // image count of the previous host-pointer step
   int hsame = 0;      // consecutive host-pointer steps with that count
   PipeConfig pipe{};  // launch shape of the FP32/FP16 collide kernel
+  long long full_wait_limit = 0;  // the collide pipeline consumers' wait limit (0: default)
   float tune_ms[LBMPSM_TUNE_CANDIDATES] = {-1.f, -1.f, -1.f, -1.f};
   bool tune_pending = false;  // the collide autotuner has yet to run
   int graph_n = -1;
@@ -398,6 +399,7 @@ int collide(lbmpsm_handle* h) {
   p.scale16 = h->scale16;
   p.status = h->d_status;
   p.pipe = h->pipe;
+  p.full_wait_limit = h->full_wait_limit;
   const int odd = (int)(h->t & 1);
   cudaError_t e;
   switch (h->opt.storage) {
@@ -848,6 +850,11 @@ int create_impl(int nbox, const lbmpsm_fix_params* ps, const lbmpsm_options* opt
     // the autotuner runs at the start of the second step, when the first
     // step's map has filled the particle table
     h->tune_pending = !env && o.collide_tuning == LBMPSM_TUNE_AUTO;
+    // test hook of the bounded-wait path: LBMPSM_TEST_FULL_WAIT_LIMIT=-1 makes
+    // the pipeline's consumers give up on their first stage at once, so that a
+    // step reports LBMPSM_ERR_TIMEOUT without any wait running long
+    if (const char* wl = std::getenv("LBMPSM_TEST_FULL_WAIT_LIMIT"))
+      h->full_wait_limit = std::atoll(wl);
   }
   int rc = ensure_particles(h, std::max(o.max_images, 1), o.max_radius > 0 ? o.max_radius : 8.0 * h->dx);
   if (rc) {
@@ -1075,13 +1082,16 @@ int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const dou
     if (h->hgraph_n != n) drop_host_graphs(h);
     const int par = (int)(h->t & 1);
     if (!h->hexec[par]) {
-      cudaGraph_t graph;
+      cudaGraph_t graph = nullptr;
       CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
       const long long t0 = h->t;
       rc = enqueue_all();
       cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
       h->t = t0;  // captured, not run
-      if (rc) return rc;
+      if (rc) {
+        if (ce == cudaSuccess && graph) cudaGraphDestroy(graph);
+        return rc;
+      }
       CUDA_TRY(h, ce);
       cudaError_t ie = cudaGraphInstantiate(&h->hexec[par], graph, 0);
       cudaGraphDestroy(graph);
@@ -1295,13 +1305,16 @@ int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps) {
   for (int s = 0; s < nsteps; ++s) {
     const int par = (int)(h->t & 1);
     if (!h->gexec[par]) {
-      cudaGraph_t graph;
+      cudaGraph_t graph = nullptr;
       CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
       const long long t0 = h->t;
       int rc = enqueue_step(h, n, use_bc);
       cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
       h->t = t0;  // captured, not run
-      if (rc) return rc;
+      if (rc) {
+        if (ce == cudaSuccess && graph) cudaGraphDestroy(graph);
+        return rc;
+      }
       CUDA_TRY(h, ce);
       cudaError_t ie = cudaGraphInstantiate(&h->gexec[par], graph, 0);
       cudaGraphDestroy(graph);
@@ -1366,7 +1379,9 @@ extern "C" int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, doub
   if (!h) return LBMPSM_ERR_ARG;
   if (h->device < 0 || h->device >= kExportMaxDevices)
     return fail(h, LBMPSM_ERR_ARG, "lbmpsm_export_fields_static: device index out of range");
-  const Geom& g = h->g;
+  // the selected box of an ensemble, exactly as lbmpsm_export_fields addresses it
+  const Geom g = box_geom(h);
+  const long long base = box_base(h);
   const size_t npts = (size_t)(g.L[0] - 2) * (g.L[1] - 2) * (g.dim == 3 ? g.L[2] - 2 : 1);
   const size_t es = as_double ? 8 : 4;
   // only the requested fields are staged, packed solid | rho | u
@@ -1392,9 +1407,9 @@ extern "C" int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, doub
   char* d_solid = solid ? b : nullptr;
   char* d_rho = rho ? b + b_solid : nullptr;
   char* d_u = u ? b + b_solid + b_rho : nullptr;
-  CUDA_TRY(h, launch_export_fields(g, h->tab, h->macro_valid ? h->rho : nullptr,
-                                   h->macro_valid ? h->u : nullptr, as_double, B0, rho0, u0,
-                                   d_solid, d_rho, d_u, h->stream));
+  CUDA_TRY(h, launch_export_fields(g, box_table(h), h->macro_valid ? h->rho + base : nullptr,
+                                   h->macro_valid ? h->u + 3 * base : nullptr, as_double, B0,
+                                   rho0, u0, d_solid, d_rho, d_u, h->stream));
   if (solid) CUDA_TRY(h, cudaMemcpyAsync(solid, d_solid, b_solid, cudaMemcpyDeviceToHost, h->stream));
   if (rho) CUDA_TRY(h, cudaMemcpyAsync(rho, d_rho, b_rho, cudaMemcpyDeviceToHost, h->stream));
   if (u) CUDA_TRY(h, cudaMemcpyAsync(u, d_u, b_u, cudaMemcpyDeviceToHost, h->stream));

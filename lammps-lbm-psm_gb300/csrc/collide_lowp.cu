@@ -338,9 +338,19 @@ __device__ __forceinline__ bool named_bar_and(int id, int nthreads, bool v) {
       : "memory");
   return r != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase) {
-  for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase,
+                                                  long long limit = MBAR_SPIN_LIMIT) {
+  for (long long it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+// The same wait, also ended when *abort (a shared-memory flag) is set.
+__device__ __forceinline__ bool mbar_wait_abortable(unsigned bar, unsigned phase,
+                                                    const volatile int* abort) {
+  for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it) {
+    if (mbar_try_wait(bar, phase)) return true;
+    if (*abort) return false;
+  }
   return false;
 }
 
@@ -359,7 +369,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase) 
 // The A-A pattern makes each block the only reader and writer of the
 // locations it moves, so blocks never wait for one another.  Every wait is
 // bounded: on expiry the block records STATUS_TIMEOUT, lets the copies it
-// issued land (bounded too) and returns.
+// issued land (bounded too) and returns.  Consumers that give up on a stage
+// (after p.full_wait_limit polls) raise a shared abort flag, which ends the
+// producer's wait for their signal at once; the producer then waits, with
+// its own long limit, only for the loads it has issued.
 template <class L, typename T, bool ODD, bool FORCE, int NST, int MINB>
 __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel(CollideParams p) {
   static_assert(NST >= 2, "stages");
@@ -367,6 +380,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
   static_assert(Q <= 32, "one producer lane per direction");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long full[NST], done[NST];
+  __shared__ int s_abort;  // set by the consumers when they give up
   const Geom& g = p.g;
   const int P0 = g.P0, S0 = g.S[0], S1 = g.S[1];
   const int R = S1 * g.S[2];
@@ -385,6 +399,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
       mbar_init(smem_addr(&full[s]), 1);
       mbar_init(smem_addr(&done[s]), (unsigned)ncons);
     }
+    s_abort = 0;
     fence_mbar_init();
   }
   __syncthreads();
@@ -414,7 +429,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
       if (!can_load) {
         // store the oldest row once the consumers are done with it
         // one decision for the whole warp (its lanes poll independently)
-        ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_addr(&done[ss]), sph));
+        ok = __all_sync(0xffffffffu, mbar_wait_abortable(smem_addr(&done[ss]), sph, &s_abort));
         if (!ok) break;
         long long base = 0;
         const bool ex = mine && (ODD ? row_of(g, sy, sz, ey, ez, base)
@@ -495,9 +510,16 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
       }
     }
     bool ok = true;
-    if (tid == 0) ok = mbar_wait_bounded(smem_addr(&full[s]), ph);
+    if (tid == 0)
+      ok = mbar_wait_bounded(smem_addr(&full[s]), ph,
+                             p.full_wait_limit > 0 ? p.full_wait_limit
+                                                   : (p.full_wait_limit < 0 ? 0 : MBAR_SPIN_LIMIT));
     if (!named_bar_and(1, ncons, ok)) {
-      if (tid == 0) atomicOr(p.status, STATUS_TIMEOUT);
+      if (tid == 0) {
+        atomicOr(p.status, STATUS_TIMEOUT);
+        *static_cast<volatile int*>(&s_abort) = 1;
+        __threadfence_block();
+      }
       return;
     }
     T* buf = reinterpret_cast<T*>(smem_raw + (size_t)s * stage_bytes);

@@ -222,6 +222,9 @@ struct CollideParams {
   int* status;            // error word (STATUS_*)
   PipeConfig pipe;
   const void* fsrc;       // FP64 only: read the populations here and write f (null: in place)
+  long long full_wait_limit;  // polls of the row pipeline's consumers on a stage's arrival
+                              // before they give up (STATUS_TIMEOUT): 0 = the default limit,
+                              // < 0 = none at all (give up at once; a test of the timeout path)
 };
 
 

@@ -17,7 +17,9 @@
 //   dem none|nve        none: atoms held in place; nve: explicit update with the
 //                       hydrodynamic force and torque (sphere mass and inertia from
 //                       density), periodic wrap
-//   output FILE         per LBM step: "step N", then per owned atom: tag F[3] T[3]
+//   output FILE         per timestep: "step N", then per owned atom: tag F[3] T[3]
+//                       (the coupling steps' forces and, on the timesteps between
+//                       them, the stored forces the fix re-applies)
 //   run N
 //
 // Per timestep, in LAMMPS' order: ghost images of the owned atoms, pre_force
@@ -198,7 +200,7 @@ int run(const std::string& path, bool check_only) {
     if (f.vti) f.vti->before_lbm_step(t);
     f.lbm->post_force(t, a);
     if (f.bc) f.bc->post_force(t);
-    if (out && t % f.lbm->nevery == 0) {
+    if (out) {
       std::fprintf(out, "step %ld\n", t);
       for (int i = 0; i < a.nlocal; ++i) {
         std::fprintf(out, "%d", a.tag[i]);

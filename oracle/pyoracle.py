@@ -16,7 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 RESTATEMENT_SO = os.path.join(HERE, "liblbmpsm_oracle.so")
 REFERENCE_SO = os.path.join(HERE, "_ref", "libref_oracle.so")
-REFERENCE_SRC = os.environ.get("LBMPSM_REFERENCE_SRC", "/root/reference/src")
+# the reference checkout beside this repository, unless LBMPSM_REFERENCE_SRC names it
+REFERENCE_SRC = os.environ.get("LBMPSM_REFERENCE_SRC",
+                               os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src"))
 
 
 class OrcParams(C.Structure):
@@ -229,3 +231,73 @@ def reverse_comm(vals: np.ndarray, owner, swap, nlocal, kind="restatement") -> n
     owner = np.ascontiguousarray(owner, dtype=np.int32); swap = np.ascontiguousarray(swap, dtype=np.int32)
     lib.orc_reverse_comm(n, nlocal, _p(owner, _I), _p(swap, _I), width, _p(vals))
     return vals
+
+
+class FixOracle:
+    """fix_LBM_PSM on one process (TEST INFRASTRUCTURE): the coupling
+    bookkeeping of src/fix_LBM_PSM.cpp around an oracle lattice.
+
+    init (src/fix_LBM_PSM.cpp:104-177): the lattice, and the DEM timestep
+    update->dt = phys_time(1)/nevery (:120), returned.
+    post_force (src/fix_LBM_PSM.cpp:181-266), given the step number and the
+    LAMMPS images (locals first, then ghosts, with the owner/swap bookkeeping
+    of make_ghosts) and the atoms' f and torque arrays (n x 3, modified in
+    place):
+      * ntimestep % nevery != 0: the stored hydrodynamic force and torque are
+        added to the local atoms (:183-196);
+      * else: one coupling step (map, halo, collide, per-image F/T/S); locals
+        f += fh, ghosts f = fh (the same for torque); the per-image F/T are
+        stored for the steps in between (:252-257); the stresslets are summed
+        as v_tally would (:259); then reverse_comm adds the ghost rows into
+        their owners (:263).
+    apply_bc is fix_LBM_PSM_BC::post_force, which runs on the same steps
+    (src/fix_LBM_PSM_BC.cpp:151-156).
+    """
+
+    def __init__(self, kind: str = "restatement", **params):
+        self.params = params
+        self.nevery = int(params.get("nevery", 1))
+        self.kind = kind
+        self.sim = None
+        self.hydrodynamicInteractions = np.zeros((0, 6))
+        self.virial = np.zeros(6)
+
+    def init(self) -> float:
+        if self.sim is not None:
+            self.sim.close()
+        self.sim = Sim(self.kind, **self.params)
+        self.hydrodynamicInteractions = np.zeros((0, 6))
+        return self.sim.info.dt_dem
+
+    def post_force(self, ntimestep: int, img: dict, f: np.ndarray, torque: np.ndarray):
+        nl = img["nlocal"]
+        if ntimestep % self.nevery:
+            hi = self.hydrodynamicInteractions
+            for i in range(nl):
+                f[i] += hi[i, :3]
+                torque[i] += hi[i, 3:]
+            return None
+        fh, th, S = self.sim.step(img["tag"], img["x"], img["v"], img["omega"], img["radius"])
+        n = len(img["tag"])
+        for i in range(n):
+            if i < nl:
+                f[i] += fh[i]
+                torque[i] += th[i]
+            else:
+                f[i] = fh[i]
+                torque[i] = th[i]
+        self.hydrodynamicInteractions = np.concatenate([fh, th], axis=1)
+        self.virial = S.sum(axis=0)
+        f[:] = reverse_comm(f, img["owner"], img["swap"], nl, self.kind)
+        torque[:] = reverse_comm(torque, img["owner"], img["swap"], nl, self.kind)
+        return fh, th, S
+
+    def apply_bc(self, ntimestep: int):
+        if ntimestep % self.nevery:
+            return
+        self.sim.apply_bc()
+
+    def close(self):
+        if self.sim is not None:
+            self.sim.close()
+            self.sim = None

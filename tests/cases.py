@@ -2,11 +2,16 @@
 (oracle/) and the GPU library, step by step, in the call order of the
 reference fixes (lbm-psm post_force, then lbm-psm-bc post_force).
 
-All cases use lattice units (dx = 1, dt = 1): rho = 1, nu = (tau-1/2)/3,
+Most cases use lattice units (dx = 1, dt = 1): rho = 1, nu = (tau-1/2)/3,
 lc = Nlc - 1 and Re = u_lb*lc/nu, which makes every unit factor 1 up to
-rounding.  Particles are placed by a seeded random sequential addition and
-moved by a prescribed velocity each step (the DEM integration is the host's
-job and is not part of the path).
+rounding.  The cases with ``phys`` set run in SI units, as the reference's
+own decks do (benchmark/in.lbmpsm_1:8-40: lc 0.0005 m, rho 1000 kg/m^3,
+nu 1e-4 m^2/s, Re 0.1): lattice spacing lc/(Nlc-1), a non-zero box origin,
+particle sizes, positions, velocities (m/s) and spins (rad/s) in physical
+units, so that every unit factor of UnitConversion is exercised.  Particles
+are placed by a seeded random sequential addition and moved by a prescribed
+velocity each step, x += v*dt_move (the DEM integration is the host's job
+and is not part of the path).
 """
 from __future__ import annotations
 
@@ -44,21 +49,34 @@ class Case:
     min_gap: float = 0.0
     cutghost: float = 0.0
     boxlo: tuple = (0.0, 0.0, 0.0)
+    phys: dict = None     # SI units: lc, rho, nu, Re (F is then Fext in N/m^3)
+    dt_move: float = 1.0  # time per step of the prescribed motion (SI cases: the DEM dt)
+
+    @property
+    def dx(self) -> float:
+        """Lattice spacing lc/(Nlc-1) (exactly 1.0 for the lattice-unit cases)."""
+        lc = self.phys["lc"] if self.phys else float(self.Nlc - 1)
+        return lc / (self.Nlc - 1)
 
     def params(self) -> dict:
-        lc = float(self.Nlc - 1)
-        nu = (self.tau - 0.5) / 3.0
-        Re = self.u_lb * lc / nu
+        if self.phys:
+            lc, rho, nu, Re = (self.phys[k] for k in ("lc", "rho", "nu", "Re"))
+        else:
+            lc = float(self.Nlc - 1)
+            rho = 1.0
+            nu = (self.tau - 0.5) / 3.0
+            Re = self.u_lb * lc / nu
+        dx = self.dx
         prd = []
         for d in range(3):
             if d >= self.dim:
-                prd.append(1.0)
+                prd.append(dx)
             else:
                 # periodic: n nodes span n*dx; walls: n nodes span (n-1)*dx
-                prd.append(float(self.n[d]) if self.periodic[d] else float(self.n[d] - 1))
-        # volumeForceFactor is 1 in these units, so Fext = F_lbm
+                prd.append(self.n[d] * dx if self.periodic[d] else (self.n[d] - 1) * dx)
+        # lattice units: volumeForceFactor is 1, so Fext = F_lbm
         return dict(dimension=self.dim, boxlo=self.boxlo, prd=tuple(prd), periodic=self.periodic,
-                    nevery=1, Nlc=self.Nlc, lc=lc, rho=1.0, nu=nu, Re=Re, tau=self.tau,
+                    nevery=1, Nlc=self.Nlc, lc=lc, rho=rho, nu=nu, Re=Re, tau=self.tau,
                     Fext=self.F)
 
 
@@ -96,7 +114,7 @@ def initial_particles(case: Case):
         margin = np.zeros(3)
         for d in range(case.dim):
             if not case.periodic[d]:
-                margin[d] = case.diam[1] / 2 + 2.0
+                margin[d] = case.diam[1] / 2 + 2.0 * case.dx
         x, r = rsa(rng, case.nparts, case.diam, lo + margin, hi - margin, case.dim, case.min_gap)
     n = len(x)
     v = rng.normal(0.0, 1.0, (n, 3)) * case.vel
@@ -114,7 +132,7 @@ def initial_particles(case: Case):
 def advance(case: Case, x, v):
     """Prescribed motion: x += v, wrapped into the box along periodic axes."""
     p = case.params()
-    x = x + v
+    x = x + v * case.dt_move
     for d in range(case.dim):
         if case.periodic[d]:
             lo = case.boxlo[d]
@@ -123,8 +141,23 @@ def advance(case: Case, x, v):
 
 
 def cutghost(case: Case) -> float:
-    return case.cutghost if case.cutghost > 0 else case.diam[1] / 2 + 3.0
+    return case.cutghost if case.cutghost > 0 else case.diam[1] / 2 + 3.0 * case.dx
 
+
+def phys_dt(Nlc, lc, nu, Re, tau, nevery=1, rho=None):
+    """The DEM timestep fix_LBM_PSM::init sets, phys_time(1)/nevery
+    (src/fix_LBM_PSM.cpp:120, src/LBM_PSM_unitConversion.cpp:22-31)."""
+    nu_lb = (tau - 0.5) * (1.0 / 3.0)
+    Uc = Re * nu / lc
+    u_lb = Re * nu_lb / (Nlc - 1)
+    dt_d = (1.0 / (Nlc - 1)) * u_lb / 1.0
+    return (1.0 * dt_d * (lc / Uc)) / nevery
+
+
+# the reference's benchmark deck units (benchmark/in.lbmpsm_1:8-40), Nlc 11
+PHYS_DECK = dict(lc=0.0005, rho=1000.0, nu=1e-4, Re=0.1)
+# an air-like 2-D channel in SI units
+PHYS_AIR = dict(lc=0.002, rho=1.2, nu=1.5e-5, Re=1.0)
 
 CASES = {
     # C1 at reduced size: D2Q9 periodic, tau 0.65, Guo force, one fixed disc of D=16
@@ -169,6 +202,18 @@ CASES = {
     "dense_periodic_2d": Case("dense_periodic_2d", 2, (30, 30, 1), (1, 1, 1), 0.6,
                               (1e-6, 1e-6, 0.0), 0, 40, nparts=10, diam=(4.0, 8.0), vel=0.1,
                               spin=0.02, seed=17, min_gap=-1.5),
+    # SI units of the benchmark deck: dx = 5e-5 m, shear walls in y, origin off
+    # zero, Fext in N/m^3 (F_lbm ~ 1e-6), spheres of 0.3-0.4 mm moving at ~1 m/s
+    # (~0.03 lattice units per step) and spinning at ~6000 rad/s, crossing x/z seams
+    "phys_shear_3d": Case("phys_shear_3d", 3, (24, 20, 24), (1, 0, 1), 0.7, (1.8e4, 0.0, -9e3),
+                          1, 30, Nlc=11, nparts=4, diam=(3e-4, 4e-4), vel=1.0, spin=6000.0,
+                          seed=21, min_gap=2.5e-5, boxlo=(-3.7e-4, 1.3e-4, 2.05e-3),
+                          phys=PHYS_DECK, dt_move=phys_dt(11, **PHYS_DECK, tau=0.7)),
+    # SI units in 2-D: channel walls, z origin ignored (origin[2] = 0 in 2-D)
+    "phys_channel_2d": Case("phys_channel_2d", 2, (40, 24, 1), (1, 0, 1), 0.8, (3.5e-3, 1e-3, 0.0),
+                            3, 40, Nlc=9, nparts=3, diam=(1e-3, 2e-3), vel=0.018, spin=24.0,
+                            seed=22, min_gap=1e-4, boxlo=(0.31, -0.07, 0.5), phys=PHYS_AIR,
+                            dt_move=phys_dt(9, **PHYS_AIR, tau=0.8)),
 }
 
 # cases whose particle boxes never reach a periodic seam: the whole state is

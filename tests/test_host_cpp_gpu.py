@@ -24,9 +24,14 @@ from lbmpsm.host import (Domain, FixLbmPsm, FixLbmPsmBC, FixLbmPsmRestart, FixLb
 pytestmark = pytest.mark.gpu
 
 DRIVER = os.path.join(cases.ROOT, "lammps-lbm-psm_gb300", "lbmpsm_driver")
-STEPS, NEVERY, CUT = 12, 1, 6.5
-FIX = ["1", "all", "lbm-psm", "every", str(NEVERY), "Nlc", "9", "lc", "8.0", "rho", "1.0",
-       "nu", repr(0.15 / 3), "Re", repr(0.01 * 8 / (0.15 / 3)), "tau", "0.65"]
+CUT = 6.5
+
+
+def _fix_args(nevery):
+    return ["1", "all", "lbm-psm", "every", str(nevery), "Nlc", "9", "lc", "8.0", "rho", "1.0",
+            "nu", repr(0.15 / 3), "Re", repr(0.01 * 8 / (0.15 / 3)), "tau", "0.65"]
+
+
 BC = ["2", "all", "lbm-psm-bc", "shear"]
 VTI = ["3", "all", "lbm-psm-vti", "every", "5", "binary", "1", "useDouble", "0"]
 RST = ["4", "all", "lbm-psm-restart", "every", "10", "write", "1", "read", "0"]
@@ -60,9 +65,15 @@ def _dem(dom, dt, dens, x, v, w, r, f, t):
             x[i, c] = xc
 
 
-def test_cpp_host_equals_python_host(tmp_path):
+@pytest.mark.parametrize("nevery,STEPS", [(1, 12), (5, 23)])
+def test_cpp_host_equals_python_host(tmp_path, nevery, STEPS):
+    """every 1, and every 5 as in the reference's fluidised-bed example
+    (examples/fluidisedBed-3D/in.lbmpsm:32): the four timesteps between
+    coupling steps re-apply the stored forces (src/fix_LBM_PSM.cpp:183-196)
+    and the DEM timestep is phys_time(1)/5 (src/fix_LBM_PSM.cpp:120)."""
     if not os.path.exists(DRIVER):
         pytest.skip("lbmpsm_driver not built")
+    FIX = _fix_args(nevery)
     tag, x, v, w, r, dens = _atoms()
     cdir = tmp_path / "cpp"
     pdir = tmp_path / "py"
@@ -109,12 +120,13 @@ def test_cpp_host_equals_python_host(tmp_path):
         nl = a.nlocal
         py = np.concatenate([tag[:, None], a.f[:nl], a.torque[:nl]], axis=1)
         assert np.array_equal(np.array(cpp[t]), py), t
-        assert np.abs(py[:, 1:4]).max() > 0
+        assert np.abs(py[:, 1:4]).max() > 0  # the stored forces on the steps in between
         _dem(dom, dt, dens, x, v, w, r, a.f[:nl], a.torque[:nl])
 
     cv = sorted(os.listdir(cdir / "flow_field_output_data"))
     pv = sorted(os.listdir(pdir / "flow_field_output_data"))
-    assert cv == pv and len(cv) == 6  # steps 0, 5, 10: one piece and one master file each
+    # every 5 steps: one piece and one master file each
+    assert cv == pv and len(cv) == 2 * len(range(0, STEPS, 5))
     for name in cv:
         assert (cdir / "flow_field_output_data" / name).read_bytes() == \
             (pdir / "flow_field_output_data" / name).read_bytes(), name

@@ -25,8 +25,10 @@ TOL_POP_SEAM = 1e-13
 
 
 def fts_scales(fh, th, S, radius):
+    # torque and stresslet are lever arm x force: their rounding scales with
+    # the largest radius (in the case's own units) times the largest force
     sF = max(np.abs(fh).max(), 1e-300)
-    rmax = max(float(np.max(radius)), 1.0)
+    rmax = float(np.max(radius))
     sT = max(np.abs(th).max(), rmax * sF)
     sS = max(np.abs(S).max(), rmax * sF)
     return sF, sT, sS
@@ -84,7 +86,7 @@ def golden():
 
 
 @pytest.mark.parametrize("name", ["c1_disc_2d", "c2_sphere_3d", "shear_3d", "dense_periodic_3d",
-                                  "closedbox_3d", "xflow_2d"])
+                                  "closedbox_3d", "xflow_2d", "phys_shear_3d", "phys_channel_2d"])
 def test_fp64_against_reference_golden(name, golden):
     """Direct check against fixtures generated by the reference's own code."""
     case = cases.CASES[name]
@@ -96,7 +98,7 @@ def test_fp64_against_reference_golden(name, golden):
     r = np.max(golden[f"{name}/r0"])
     sF = np.abs(ref[:, :3]).max()
     assert np.abs(fts[:, :3] - ref[:, :3]).max() <= TOL_FTS * sF
-    assert np.abs(fts[:, 3:] - ref[:, 3:]).max() <= TOL_FTS * max(r, 1.0) * sF * 10
+    assert np.abs(fts[:, 3:] - ref[:, 3:]).max() <= TOL_FTS * r * sF * 10
     f = gpu.lat.populations().reshape(-1, gpu.lat.q)
     np.testing.assert_allclose(f[golden[f"{name}/sample"]], golden[f"{name}/fpop"], rtol=1e-12, atol=0)
 

@@ -104,3 +104,45 @@ def test_requests_beyond_the_fixed_array_are_rejected():
     exp = lat.export_fields(1.0, 1.0, 1.0, as_double=False)
     for k, e in zip(("solid", "rho", "u"), exp):
         assert np.array_equal(got[k], e), k
+
+
+def test_selected_box_of_an_ensemble_equals_the_allocating_export():
+    # three periodic boxes of one geometry but different tau, force and
+    # particles; each selected box (the last ones especially, whose planes
+    # sit furthest from the start of the allocation) must export its own
+    # fields, as lbmpsm_export_fields does
+    edge = 16
+    boxes, parts = [], []
+    for b, (tau, fx) in enumerate([(0.7, 1e-6), (0.9, 6e-6), (0.62, 3e-6)]):
+        nu = (tau - 0.5) / 3.0
+        boxes.append(dict(dimension=3, boxlo=(0.0, 0.0, 0.0), prd=(float(edge),) * 3,
+                          periodic=(1, 1, 1), Nlc=9, lc=8.0, rho=1.0, nu=nu, Re=0.01 * 8 / nu,
+                          tau=tau, Fext=(fx, 0.0, 0.0)))
+        rng = np.random.default_rng(300 + b)
+        x, r = cases.rsa(rng, 1 + b, (4.0, 6.0), np.zeros(3) + 3.0, np.zeros(3) + edge - 3.0, 3,
+                         min_gap=0.5)
+        parts.append((np.arange(1, len(x) + 1, dtype=np.int32), x, r))
+    ens = lbmpsm.Ensemble(boxes, storage="fp64")
+    cols = {k: [] for k in ("box", "tag", "x", "r")}
+    for b, (tag, x, r) in enumerate(parts):
+        cols["box"].append(np.full(len(tag), b, np.int32))
+        cols["tag"].append(tag)
+        cols["x"].append(x)
+        cols["r"].append(r)
+    c = {k: np.concatenate(v) for k, v in cols.items()}
+    z = np.zeros_like(c["x"])
+    for s in range(6):
+        if s == 5:
+            ens.request_macro()
+        ens.step(c["box"], c["tag"], c["x"], z, z, c["r"])
+    seen = []
+    for b in (2, 1, 0):
+        ens.select_box(b)
+        code, got = export_static(ens, 1.0, 1000.0, 3.0, as_double=True)
+        assert code == lbmpsm.OK, ens.lib.lbmpsm_last_error(ens.h)
+        exp = ens.export_fields(1.0, 1000.0, 3.0, as_double=True)
+        for k, e in zip(("solid", "rho", "u"), exp):
+            assert np.array_equal(got[k], e), (b, k)
+        seen.append(got["u"].copy())
+    # the boxes differ (tau, force, particles), so box selection is visible
+    assert not np.array_equal(seen[0], seen[2])
