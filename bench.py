@@ -47,7 +47,7 @@ U_WALL = 0.01
 SEED = 20261203
 METRIC = "D3Q19 PSM MLUPS & % HBM roofline, FP32 vs FP64 at fixed drag error, 1 GB300"
 REF_MAX_STEPS = 20
-BYTES_PER_NODE = {"fp64": 2 * 19 * 8, "fp32": 2 * 19 * 4, "fp16": 2 * 19 * 2}
+BYTES_PER_NODE = {"fp64": 2 * 19 * 8, "fp32": 2 * 19 * 4, "fp16": 2 * 19 * 2, "bf16": 2 * 19 * 2}
 
 
 def workload_params(edge=None):
@@ -851,7 +851,7 @@ def main():
                     help="steps of the single-sphere accuracy run")
     ap.add_argument("--edge", type=int, default=EDGE, help="lattice edge (profiling cases)")
     ap.add_argument("--nspheres", type=int, default=NSPHERES)
-    ap.add_argument("--storage", choices=["fp32", "fp16"], default="fp32")
+    ap.add_argument("--storage", choices=["fp32", "fp16", "bf16"], default="fp32")
     ap.add_argument("--workload", choices=["suspension", "ensemble", "adjoint"], default="suspension",
                     help="suspension: the headline line; ensemble: the batched-box workload; "
                          "adjoint: the drag-sensitivity sweep")

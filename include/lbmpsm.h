@@ -53,6 +53,7 @@ extern "C" {
 #define LBMPSM_STORAGE_FP64 0 /* plain FP64, the reference arithmetic */
 #define LBMPSM_STORAGE_FP32 1 /* FP32 deviations f_i - w_i*rho0, FP32 collision */
 #define LBMPSM_STORAGE_FP16 2 /* FP16 scaled deviations, FP32 collision */
+#define LBMPSM_STORAGE_BF16 3 /* BF16 deviations, FP32 collision */
 
 /* `fix lbm-psm-bc` keywords (src/fix_LBM_PSM_BC.cpp:21-39) */
 #define LBMPSM_BC_NONE 0

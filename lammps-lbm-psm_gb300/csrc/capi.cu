@@ -82,6 +82,7 @@ struct lbmpsm_handle {
   int hsame = 0;      // consecutive host-pointer steps with that count
   PipeConfig pipe{};  // launch shape of the FP32/FP16 collide kernel
   long long full_wait_limit = 0;  // the collide pipeline consumers' wait limit (0: default)
+
   float tune_ms[LBMPSM_TUNE_CANDIDATES] = {-1.f, -1.f, -1.f, -1.f};
   bool tune_pending = false;  // the collide autotuner has yet to run
   int graph_n = -1;
@@ -129,7 +130,7 @@ void dfree(void* p) {
   if (p) cudaFree(p);
 }
 
-size_t storage_bytes(int storage) { return storage == 0 ? 8 : (storage == 1 ? 4 : 2); }
+size_t storage_bytes(int storage) { return storage == 0 ? 8 : (storage == 1 ? 4 : 2); }  // FP16, BF16: 2
 
 // Zou-He face calls of fix_LBM_PSM_BC::post_force (src/fix_LBM_PSM_BC.cpp:223-401)
 // on one rank, converted from the reference halo frame to device storage.
@@ -405,6 +406,7 @@ int collide(lbmpsm_handle* h) {
   switch (h->opt.storage) {
     case LBMPSM_STORAGE_FP64: e = launch_collide_f64(p, odd, h->stream); break;
     case LBMPSM_STORAGE_FP32: e = launch_collide_f32(p, odd, h->stream); break;
+    case LBMPSM_STORAGE_BF16: e = launch_collide_bf16(p, odd, h->stream); break;
     default: e = launch_collide_f16(p, odd, h->stream); break;
   }
   CUDA_TRY(h, e);
@@ -566,6 +568,7 @@ int enqueue_bc(lbmpsm_handle* h, cudaStream_t st) {
   switch (h->opt.storage) {
     case LBMPSM_STORAGE_FP64: e = launch_bc_f64(b, st); break;
     case LBMPSM_STORAGE_FP32: e = launch_bc_f32(b, st); break;
+    case LBMPSM_STORAGE_BF16: e = launch_bc_bf16(b, st); break;
     default: e = launch_bc_f16(b, st); break;
   }
   CUDA_TRY(h, e);
@@ -675,7 +678,7 @@ int create_impl(int nbox, const lbmpsm_fix_params* ps, const lbmpsm_options* opt
   const lbmpsm_fix_params* p = ps;
   lbmpsm_options o{};
   if (opts) o = *opts;
-  if (o.storage < 0 || o.storage > 2)
+  if (o.storage < 0 || o.storage > 3)
     return fail(nullptr, LBMPSM_ERR_ARG, "unknown storage precision");
   if (o.psm_weighting < 0 || o.psm_weighting > 1)
     return fail(nullptr, LBMPSM_ERR_ARG, "unknown PSM weighting");

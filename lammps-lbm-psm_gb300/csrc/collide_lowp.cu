@@ -2,14 +2,16 @@
 // kernel and the Zou-He face kernel.
 //
 // Populations are stored as deviations g_q = f_q - w_q*rho0 (rho0 = 1): in
-// FP32 (LBMPSM_STORAGE_FP32) or in FP16 scaled by scale16
-// (LBMPSM_STORAGE_FP16).  The collision runs in FP32 on the deviations, which
+// FP32 (LBMPSM_STORAGE_FP32), in FP16 scaled by scale16
+// (LBMPSM_STORAGE_FP16), or in BF16 (LBMPSM_STORAGE_BF16: FP32's exponent
+// range, so no scale, and 8 significant bits against FP16's 11).  The collision runs in FP32 on the deviations, which
 // keeps the small differences f - feq of a low-Mach flow well resolved; the
 // algebra is the reference's (src/LBM_PSM_BGK_dynamics.h:40-114,
 // src/LBM_PSM_dynamics.h:43-116) with the w_q*rho0 parts cancelled:
 //   feq_q - w_q = w_q (drho + rho (3 e.u + 4.5 (e.u)^2 - 1.5 u.u)).
 // Node forces of PSM nodes are written in FP32 and reduced per particle in
 // FP64 (particles.cu).
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -24,6 +26,15 @@ template <>
 struct Store<float> {
   __device__ __forceinline__ static float load(const float* p, float) { return *p; }
   __device__ __forceinline__ static void store(float* p, float v, float) { *p = v; }
+};
+template <>
+struct Store<__nv_bfloat16> {
+  __device__ __forceinline__ static float load(const __nv_bfloat16* p, float) {
+    return __bfloat162float(*p);
+  }
+  __device__ __forceinline__ static void store(__nv_bfloat16* p, float v, float) {
+    *p = __float2bfloat16_rn(v);
+  }
 };
 template <>
 struct Store<__half> {
@@ -626,6 +637,9 @@ cudaError_t prepare_collide_lowp(const Geom& g, int storage, int sm_count, int s
   if (storage == 1)
     return g.dim == 2 ? prepare_lowp<D2Q9, float>(g, sm_count, stages, cfg)
                       : prepare_lowp<D3Q19, float>(g, sm_count, stages, cfg);
+  if (storage == 3)
+    return g.dim == 2 ? prepare_lowp<D2Q9, __nv_bfloat16>(g, sm_count, stages, cfg)
+                      : prepare_lowp<D3Q19, __nv_bfloat16>(g, sm_count, stages, cfg);
   return g.dim == 2 ? prepare_lowp<D2Q9, __half>(g, sm_count, stages, cfg)
                     : prepare_lowp<D3Q19, __half>(g, sm_count, stages, cfg);
 }
@@ -707,6 +721,8 @@ cudaError_t tune_collide_lowp(CollideParams p, int storage, int sm_count, cudaSt
       for (int odd = 0; odd < 2; ++odd)
         if (storage == 1)
           launch_collide_f32(p, odd, st);
+        else if (storage == 3)
+          launch_collide_bf16(p, odd, st);
         else
           launch_collide_f16(p, odd, st);
     };
@@ -737,6 +753,10 @@ cudaError_t launch_collide_f32(const CollideParams& p, int odd, cudaStream_t st)
 cudaError_t launch_collide_f16(const CollideParams& p, int odd, cudaStream_t st) {
   return p.g.dim == 2 ? launch_lowp<D2Q9, __half>(p, odd, st)
                       : launch_lowp<D3Q19, __half>(p, odd, st);
+}
+cudaError_t launch_collide_bf16(const CollideParams& p, int odd, cudaStream_t st) {
+  return p.g.dim == 2 ? launch_lowp<D2Q9, __nv_bfloat16>(p, odd, st)
+                      : launch_lowp<D3Q19, __nv_bfloat16>(p, odd, st);
 }
 
 // ------------------------------------------------------------------ Zou-He
@@ -939,5 +959,8 @@ static cudaError_t launch_bc_lowp(const BCParams& p, cudaStream_t st) {
 
 cudaError_t launch_bc_f32(const BCParams& p, cudaStream_t st) { return launch_bc_lowp<float>(p, st); }
 cudaError_t launch_bc_f16(const BCParams& p, cudaStream_t st) { return launch_bc_lowp<__half>(p, st); }
+cudaError_t launch_bc_bf16(const BCParams& p, cudaStream_t st) {
+  return launch_bc_lowp<__nv_bfloat16>(p, st);
+}
 
 }  // namespace lbmpsm

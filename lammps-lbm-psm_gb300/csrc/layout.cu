@@ -9,6 +9,7 @@
 // the reference never writes that entry and it keeps the initial
 // equilibrium w_q (src/LBM_PSM_BGK_dynamics.cpp:94-99 skips targets outside
 // the array).
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include "lbmpsm_internal.cuh"
@@ -21,6 +22,7 @@ __device__ __forceinline__ double load_pop(const void* f, long long loc, int sto
   (void)sizeof(T);
   if (storage == 0) return static_cast<const double*>(f)[loc];
   if (storage == 1) return w + (double)static_cast<const float*>(f)[loc];
+  if (storage == 3) return w + (double)__bfloat162float(static_cast<const __nv_bfloat16*>(f)[loc]);
   return w + (double)(__half2float(static_cast<const __half*>(f)[loc]) / scale);
 }
 
@@ -30,6 +32,8 @@ __device__ __forceinline__ void store_pop(void* f, long long loc, int storage, f
     static_cast<double*>(f)[loc] = v;
   else if (storage == 1)
     static_cast<float*>(f)[loc] = (float)(v - w);
+  else if (storage == 3)
+    static_cast<__nv_bfloat16*>(f)[loc] = __float2bfloat16_rn((float)(v - w));
   else
     static_cast<__half*>(f)[loc] = __float2half_rn((float)(v - w) * scale);
 }
@@ -53,6 +57,8 @@ __global__ void init_kernel(Geom g, void* f, int storage, float scale) {
       static_cast<double*>(f)[loc] = L::w(q);  // feq(rho = 1, u = 0) = w_q
     else if (storage == 1)
       static_cast<float*>(f)[loc] = 0.0f;
+    else if (storage == 3)
+      static_cast<__nv_bfloat16*>(f)[loc] = __float2bfloat16_rn(0.0f);
     else
       static_cast<__half*>(f)[loc] = __float2half_rn(0.0f);
   }
@@ -149,7 +155,7 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
 
 // Blocks walk x-rows with 32-bit index arithmetic (64-bit integer division
 // is emulated and slow).  FP64 storage sums the populations in FP64.  FP32 /
-// FP16 storage sums each node's deviations g = f - w in FP32 and adds the
+// FP16 / BF16 storage sums each node's deviations g = f - w in FP32 and adds the
 // node sums into double-float accumulators on the FP32 pipe; the weights add
 // up to exactly 1 per node (mass = nodes + sum g) and to 0 in every momentum
 // component.
@@ -186,8 +192,9 @@ __global__ void __launch_bounds__(CHECK_THREADS) check_partial_kernel(Geom g, co
           const long long loc = loc_of<L>(g, nb, n, q, after_odd);
           float v = 0.0f;
           if (loc >= 0)
-            v = storage == 1 ? static_cast<const float*>(f)[loc]
-                             : __half2float(static_cast<const __half*>(f)[loc]) * inv_scale;
+            v = storage == 1   ? static_cast<const float*>(f)[loc]
+                : storage == 3 ? __bfloat162float(static_cast<const __nv_bfloat16*>(f)[loc])
+                               : __half2float(static_cast<const __half*>(f)[loc]) * inv_scale;
           if (!isfinite(v)) bad = true;
           ns[0] += v;
           if (L::ex(q)) ns[1] += L::ex(q) > 0 ? v : -v;

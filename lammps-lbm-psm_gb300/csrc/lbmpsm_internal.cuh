@@ -404,7 +404,8 @@ struct AdjCentre {
 cudaError_t launch_collide_f64(const CollideParams& p, int odd, cudaStream_t st);
 cudaError_t launch_collide_f32(const CollideParams& p, int odd, cudaStream_t st);
 cudaError_t launch_collide_f16(const CollideParams& p, int odd, cudaStream_t st);
-// storage 1 (FP32) or 2 (FP16); sets the kernels' shared-memory limit and
+cudaError_t launch_collide_bf16(const CollideParams& p, int odd, cudaStream_t st);
+// storage 1 (FP32), 2 (FP16) or 3 (BF16); sets the kernels' shared-memory limit and
 // sizes the persistent grid from the occupancy on this device (stages 0:
 // the direct kernel, cfg left empty)
 cudaError_t prepare_collide_lowp(const Geom& g, int storage, int sm_count, int stages,
@@ -418,6 +419,7 @@ cudaError_t tune_collide_lowp(CollideParams p, int storage, int sm_count, cudaSt
 cudaError_t launch_bc_f64(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f32(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f16(const BCParams& p, cudaStream_t st);
+cudaError_t launch_bc_bf16(const BCParams& p, cudaStream_t st);
 // population layout conversions (storage <-> reference AoS with halo, FP64)
 cudaError_t launch_init_populations(const Geom& g, void* f, int storage, float scale16,
                                     cudaStream_t st);

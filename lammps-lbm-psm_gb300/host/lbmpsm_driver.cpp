@@ -12,7 +12,7 @@
 //   box xlo xhi ylo yhi zlo zhi
 //   atoms FILE          one atom per line: tag x y z vx vy vz wx wy wz radius density
 //   cutghost C          ghost cut-off (communicate cutoff of the LAMMPS run)
-//   storage fp64|fp32|fp16
+//   storage fp64|fp32|fp16|bf16
 //   fix ID group STYLE args...   STYLE = lbm-psm | lbm-psm-bc | lbm-psm-vti | lbm-psm-restart
 //   dem none|nve        none: atoms held in place; nve: explicit update with the
 //                       hydrodynamic force and torque (sphere mass and inertia from
@@ -86,8 +86,10 @@ Deck read_deck(const std::string& path) {
       d.cutghost = std::stod(w[1]);
     } else if (c == "storage") {
       need(2);
-      d.storage = w[1] == "fp32" ? LBMPSM_STORAGE_FP32
-                                 : (w[1] == "fp16" ? LBMPSM_STORAGE_FP16 : LBMPSM_STORAGE_FP64);
+      d.storage = w[1] == "fp32"   ? LBMPSM_STORAGE_FP32
+                  : w[1] == "fp16" ? LBMPSM_STORAGE_FP16
+                  : w[1] == "bf16" ? LBMPSM_STORAGE_BF16
+                                   : LBMPSM_STORAGE_FP64;
     } else if (c == "fix") {
       need(4);
       d.fixes.emplace_back(w.begin() + 1, w.end());  // ID group style args...

@@ -28,7 +28,7 @@ LIB_PATH = os.path.join(PKG, "liblbmpsm_gb300.so")
 OK = 0
 ERR_ARG, ERR_MACH, ERR_GRID, ERR_NOMEM, ERR_CUDA, ERR_STATE, ERR_CAPACITY, ERR_NUMERIC, ERR_TIMEOUT = (
     -1, -2, -3, -4, -5, -6, -7, -8, -9)
-STORAGE = {"fp64": 0, "fp32": 1, "fp16": 2}
+STORAGE = {"fp64": 0, "fp32": 1, "fp16": 2, "bf16": 3}
 BC = {"none": 0, "shear": 1, "xFlow": 2, "channel": 3, "channel-velIn-pressOut": 4, "closedBox": 5}
 WEIGHTING = {"reference": 0, "noble-torczynski": 1}
 TUNING = {"auto": 0, "default": 1}  # LBMPSM_TUNE_*

@@ -5,7 +5,7 @@ must evolve exactly like the same boxes run as separate lattices: the same
 kernels run on each box's planes with that box's parameters.  Checked bit
 for bit on the per-image force / torque / stresslet of every step and on
 each box's populations and particle table at the end, in FP64, FP32 and
-FP16 storage.
+FP16 and BF16 storage.
 """
 import numpy as np
 import pytest
@@ -43,7 +43,7 @@ def _images(box, tag, x, v, w, r):
                                      w, r)
 
 
-@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16"])
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16", "bf16"])
 def test_ensemble_equals_separate_lattices(storage):
     boxes = _boxes()
     ens = lbmpsm.Ensemble(boxes, storage=storage)

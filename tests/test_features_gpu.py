@@ -61,7 +61,7 @@ def test_export_fields_match_oracle():
     assert f32[0].dtype == np.float32 and np.allclose(f32[1], exp[1], rtol=1e-6)
 
 
-@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16"])
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16", "bf16"])
 def test_populations_roundtrip_and_mass_check(storage):
     case = cases.CASES["box_small_3d"]
     lat = _lat(case, storage)
@@ -71,13 +71,13 @@ def test_populations_roundtrip_and_mass_check(storage):
     lat.set_populations(f1)
     back = lat.populations()
     m = lat.stored_mask()
-    tol = {"fp64": 0.0, "fp32": 1e-8, "fp16": 1e-5}[storage]
+    tol = {"fp64": 0.0, "fp32": 1e-8, "fp16": 1e-5, "bf16": 1e-5}[storage]
     assert np.abs(back[m] - f1[m]).max() <= tol
     mass0, _ = lat.check()
     for _ in range(5):
         lat.step([], np.zeros((0, 3)), np.zeros((0, 3)), np.zeros((0, 3)), [])
     mass1, _ = lat.check()
-    assert abs(mass1 - mass0) <= {"fp64": 1e-9, "fp32": 1e-3, "fp16": 1e-1}[storage] * 1e-3 * mass0
+    assert abs(mass1 - mass0) <= {"fp64": 1e-9, "fp32": 1e-3, "fp16": 1e-1, "bf16": 1e-1}[storage] * 1e-3 * mass0
 
 
 def test_nonfinite_population_is_reported():

@@ -10,7 +10,7 @@ FP64 storage keeps the reference arithmetic:
   * per-image force, torque and stresslet within 1e-12 relative (the device
     sums node contributions in a fixed tree order, the reference
     sequentially); torque and stresslet relative to r_max*|F|_max.
-FP32 / FP16 storage: drag and torque within the tolerances stated below
+FP32 / FP16 / BF16 storage: drag and torque within the tolerances stated below
 against the FP64 device path.
 """
 import numpy as np
@@ -119,6 +119,7 @@ def _drag_run(case, storage, steps):
 @pytest.mark.parametrize("name,storage,tol", [
     ("c2_sphere_3d", "fp32", 1e-3), ("c1_disc_2d", "fp32", 1e-3), ("shear_3d", "fp32", 1e-3),
     ("closedbox_3d", "fp32", 1e-3), ("c2_sphere_3d", "fp16", 1e-1), ("shear_3d", "fp16", 1e-1),
+    ("c2_sphere_3d", "bf16", 2e-1), ("shear_3d", "bf16", 2e-1),
 ])
 def test_low_precision_storage_against_fp64(name, storage, tol):
     case = cases.CASES[name]

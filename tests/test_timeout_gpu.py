@@ -23,7 +23,7 @@ def _first_images(case):
     return cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
 
 
-@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
 def test_stage_wait_expiry_is_reported_and_a_fresh_handle_steps(storage, monkeypatch):
     case = cases.CASES["c2_sphere_3d"]
     g = _first_images(case)

@@ -33,7 +33,7 @@ def _run(case, storage, steps, **kw):
     return lat, out
 
 
-@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
 @pytest.mark.parametrize("name", ["shear_3d", "shear_2d"])
 def test_every_launch_shape_gives_the_same_results(name, storage, monkeypatch):
     case = cases.CASES[name]
