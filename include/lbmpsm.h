@@ -161,7 +161,9 @@ int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
                 const double* omega, const double* radius, double* fh, double* th,
                 double* stresslet);
 /* Same, with all arrays in device memory; asynchronous on the handle's
- * stream.  Requires opts.max_radius >= every radius. */
+ * stream.  Requires opts.max_radius >= every radius.  The outputs (each may
+ * be NULL) are written by the step's own reduction; the handle keeps a copy
+ * as well (lbmpsm_read_forces). */
 int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
                        const double* v, const double* omega, const double* radius, double* fh,
                        double* th, double* stresslet);
@@ -215,9 +217,8 @@ void* lbmpsm_stream(lbmpsm_handle* h);
 /* Run nsteps coupling steps with the particle images already on the device
  * (as last passed to lbmpsm_step or lbmpsm_step_device), fixed in place,
  * each step followed by the boundary condition when one is set.  The step
- * sequence is captured once into a CUDA graph and replayed.  Forces of the
- * last step land in the device buffers of the last step_device call (or in
- * the handle's own buffers after a host step; read with lbmpsm_read_forces). */
+ * sequence is captured once into a CUDA graph and replayed.  The forces of
+ * each step land in the handle's own buffers (read with lbmpsm_read_forces). */
 int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps);
 /* Copy the per-image outputs of the last step to host memory. */
 int lbmpsm_read_forces(lbmpsm_handle* h, int n, double* fh, double* th, double* stresslet);

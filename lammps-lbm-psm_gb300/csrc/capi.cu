@@ -98,6 +98,17 @@ struct lbmpsm_handle {
   bool step_boxes = false;   // the current images carry box indices
   bool any_force = false;
   int sel_box = 0;           // box the reference-layout calls address
+  double* out2[3]{};         // lbmpsm_step_device: the caller's F/T/S buffers, written by
+                             // the reduction beside the handle's own (null otherwise)
+  // graphs of one device-pointer step for each parity (gather of the caller's
+  // images, map + collide + reduce); the gather and reduce nodes take each
+  // call's pointers
+  cudaGraph_t dgraph[2]{nullptr, nullptr};
+  cudaGraphExec_t dexec[2]{nullptr, nullptr};
+  cudaGraphNode_t dgather[2]{nullptr, nullptr}, dreduce[2]{nullptr, nullptr};
+  int dgraph_n = -1;
+  int dprev_n = -1;  // image count of the previous device step
+  int dsame = 0;     // consecutive device steps with that count
 };
 
 namespace {
@@ -288,9 +299,21 @@ void drop_host_graphs(lbmpsm_handle* h) {
   h->hgraph_n = -1;
 }
 
+void drop_device_graphs(lbmpsm_handle* h) {
+  for (int k = 0; k < 2; ++k) {
+    if (h->dexec[k]) cudaGraphExecDestroy(h->dexec[k]);
+    if (h->dgraph[k]) cudaGraphDestroy(h->dgraph[k]);
+    h->dexec[k] = nullptr;
+    h->dgraph[k] = nullptr;
+    h->dgather[k] = h->dreduce[k] = nullptr;
+  }
+  h->dgraph_n = -1;
+}
+
 void drop_graphs(lbmpsm_handle* h) {
   drop_run_graphs(h);
   drop_host_graphs(h);
+  drop_device_graphs(h);
   h->graph_gen += 1;
 }
 
@@ -547,6 +570,9 @@ int enqueue_step(lbmpsm_handle* h, int n, bool bc = false) {
     rp.fh = h->d_out;
     rp.th = h->d_out + 3 * (size_t)n;
     rp.S = h->d_out + 6 * (size_t)n;
+    rp.fh2 = h->out2[0];
+    rp.th2 = h->out2[1];
+    rp.S2 = h->out2[2];
     CUDA_TRY(h, launch_reduce(rp, h->stream));
   }
   if (bc_aside) CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->ev_bc_join, 0));
@@ -1148,21 +1174,96 @@ int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
   }
   if (h->step_boxes) drop_graphs(h);
   h->step_boxes = false;
-  const size_t nn = (size_t)n;
-  if (n > 0) {
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_tag, tag, sizeof(int) * nn, cudaMemcpyDeviceToDevice, h->stream));
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw, x, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, h->stream));
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw + 3 * nn, v, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, h->stream));
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw + 6 * nn, omega, sizeof(double) * 3 * nn, cudaMemcpyDeviceToDevice, h->stream));
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_xvw + 9 * nn, radius, sizeof(double) * nn, cudaMemcpyDeviceToDevice, h->stream));
+  if (n > 0 && (!tag || !x || !v || !omega || !radius))
+    return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
+  // the images into the handle's buffers in one launch; the reduction writes
+  // the outputs into the caller's buffers beside the handle's own
+  auto enqueue_all = [&]() -> int {
+    CUDA_TRY(h, launch_gather_images(n, tag, x, v, omega, radius, h->d_tag, h->d_xvw, h->stream));
+    h->out2[0] = n > 0 ? fh : nullptr;
+    h->out2[1] = n > 0 ? th : nullptr;
+    h->out2[2] = n > 0 ? stresslet : nullptr;
+    const int r = enqueue_step(h, n);
+    h->out2[0] = h->out2[1] = h->out2[2] = nullptr;
+    return r;
+  };
+  // Replayed as one CUDA graph per parity once the image count has held for
+  // two calls (as host steps are); each call writes its own pointers into the
+  // gather and reduce nodes of the executable graph, which affects only the
+  // launches that follow.  Steps that store the macroscopic fields, and steps
+  // without images, run eagerly.
+  h->dsame = n == h->dprev_n ? h->dsame + 1 : 0;
+  h->dprev_n = n;
+  if (n == 0 || h->macro_requested || (h->dgraph_n != n && h->dsame < 2)) return enqueue_all();
+  if (h->dgraph_n != n) drop_device_graphs(h);
+  const int par = (int)(h->t & 1);
+  if (!h->dexec[par]) {
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long t0 = h->t;
+    const int rc = enqueue_all();
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    h->t = t0;  // captured, not run
+    if (rc) {
+      if (ce == cudaSuccess && graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CUDA_TRY(h, ce);
+    // the nodes whose arguments change per call
+    size_t nn = 0;
+    cudaError_t e = cudaGraphGetNodes(graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (e == cudaSuccess) e = cudaGraphGetNodes(graph, nodes.data(), &nn);
+    cudaGraphNode_t gn = nullptr, rn = nullptr;
+    const void* fg = gather_images_fn();
+    const void* fr = reduce_fn(h->opt.storage == LBMPSM_STORAGE_FP64 ? 1 : 0);
+    for (size_t k = 0; e == cudaSuccess && k < nn; ++k) {
+      cudaGraphNodeType ty;
+      if (cudaGraphNodeGetType(nodes[k], &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp{};
+      if (cudaGraphKernelNodeGetParams(nodes[k], &kp) != cudaSuccess) continue;
+      if (kp.func == fg) gn = nodes[k];
+      if (kp.func == fr) rn = nodes[k];
+    }
+    cudaGraphExec_t ex = nullptr;
+    if (e == cudaSuccess && gn && rn) e = cudaGraphInstantiate(&ex, graph, 0);
+    if (e != cudaSuccess || !gn || !rn) {
+      cudaGetLastError();
+      cudaGraphDestroy(graph);
+      CUDA_TRY(h, e);
+      return fail(h, LBMPSM_ERR_CUDA, "device-step graph: the gather or reduce node was not found");
+    }
+    h->dgraph[par] = graph;
+    h->dexec[par] = ex;
+    h->dgather[par] = gn;
+    h->dreduce[par] = rn;
+    h->dgraph_n = n;
   }
-  int rc = enqueue_step(h, n);
-  if (rc) return rc;
-  if (n > 0) {
-    if (fh) CUDA_TRY(h, cudaMemcpyAsync(fh, h->d_out, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, h->stream));
-    if (th) CUDA_TRY(h, cudaMemcpyAsync(th, h->d_out + 3 * (size_t)n, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, h->stream));
-    if (stresslet) CUDA_TRY(h, cudaMemcpyAsync(stresslet, h->d_out + 6 * (size_t)n, sizeof(double) * 6 * n, cudaMemcpyDeviceToDevice, h->stream));
+  {
+    // this call's pointers into the gather and reduce nodes
+    cudaKernelNodeParams kp{};
+    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dgather[par], &kp));
+    int* dt = h->d_tag;
+    double* dxvw = h->d_xvw;
+    void* ga[] = {(void*)&n, (void*)&tag, (void*)&x, (void*)&v, (void*)&omega, (void*)&radius,
+                  (void*)&dt, (void*)&dxvw};
+    kp.kernelParams = ga;
+    kp.extra = nullptr;
+    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dgather[par], &kp));
+    cudaKernelNodeParams rk{};
+    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dreduce[par], &rk));
+    ReduceParams rp = *static_cast<const ReduceParams*>(rk.kernelParams[0]);
+    rp.fh2 = fh;
+    rp.th2 = th;
+    rp.S2 = stresslet;
+    void* ra[] = {(void*)&rp};
+    rk.kernelParams = ra;
+    rk.extra = nullptr;
+    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dreduce[par], &rk));
   }
+  CUDA_TRY(h, cudaGraphLaunch(h->dexec[par], h->stream));
+  h->t += 1;
+  h->last_n = n;
   return LBMPSM_OK;
 }
 

@@ -331,6 +331,9 @@ struct ReduceParams {
   double* fh;
   double* th;
   double* S;
+  double* fh2;        // optional second copies of the outputs (the caller's device
+  double* th2;        // buffers of lbmpsm_step_device), written with the first
+  double* S2;
 };
 
 // status bits
@@ -435,6 +438,14 @@ cudaError_t launch_check(const Geom& g, const void* f, int storage, int after_od
 cudaError_t launch_map(const MapParams& p, cudaStream_t st, cudaStream_t aux = nullptr,
                        cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st);
+// the kernels whose arguments a replayed device-step graph updates per call
+const void* gather_images_fn();
+const void* reduce_fn(int nodeF_is_double);
+// the image arrays of lbmpsm_step_device into the handle's image buffers
+// (tag[n]; x | v | omega (3n each) | radius (n)) in one launch
+cudaError_t launch_gather_images(int n, const int* tag, const double* x, const double* v,
+                                 const double* omega, const double* radius, int* d_tag,
+                                 double* d_xvw, cudaStream_t st);
 cudaError_t launch_table_export(const Geom& g, const Table& t, int* ids, double* eps,
                                 double* us, cudaStream_t st);
 cudaError_t launch_export_fields(const Geom& g, const Table& t, const double* rho,

@@ -977,36 +977,44 @@ static __device__ __forceinline__ float4 spin_velocity(const Img& im, int hi, in
 // are visited in image order through their compact records, which cell_sort
 // copied next to the list entries (three 16-byte loads straight after the
 // cell's offset, instead of list index, then record, then the scattered
-// fields of Img), each record serving all the thread's nodes, whose code,
-// slot id and slot record loads are independent; the slot ids are loaded on
-// first use only.
+// fields of Img), each record serving all the thread's nodes, whose code
+// and slot record loads are independent.  The slot ids are loaded with the
+// cell's count and offset, so that they add no round of dependent loads.
 template <int NPT>
 __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p) {
   const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
-  const int cnt = p.cell_count[c];
-  if (cnt == 0) return;
-  if (p.pair_total[0] > (unsigned long long)p.list_cap ||
-      p.pair_total[1] > (unsigned long long)p.sf_cap)
-    return;
   const Geom& g = p.g;
   const int sx = blockIdx.x * p.cb[0] + threadIdx.x;
   const int sy = blockIdx.y * p.cb[1] + threadIdx.y;
   const int sz0 = blockIdx.z * p.cb[2] + threadIdx.z;
-  if (sx >= g.S[0] || sy >= g.S[1] || sz0 >= g.S[2]) return;
   const int dz = (int)blockDim.z;
   const long long n0 = node_index(g, sx, sy, sz0);
   const long long zstride = (long long)dz * g.P0 * g.S[1];
+  const bool inside = sx < g.S[0] && sy < g.S[1] && sz0 < g.S[2];
   bool has[NPT];
 #pragma unroll
   for (int k = 0; k < NPT; ++k)
-    has[k] = (int)threadIdx.z + k * dz < p.cb[2] && sz0 + k * dz < g.S[2];
-  const int4* lrec = p.lrec + 3 * (long long)p.cell_off[c];
-  Apply32 st[NPT];
-  bool have[NPT];
+    has[k] = inside && (int)threadIdx.z + k * dz < p.cb[2] && sz0 + k * dz < g.S[2];
+  // the cell's count and offset, the overflow words and the slot ids of the
+  // thread's nodes: independent loads, issued together
+  const int cnt = __ldg(p.cell_count + c);
+  const int coff = __ldg(p.cell_off + c);
+  const unsigned long long tot0 = __ldg(p.pair_total), tot1 = __ldg(p.pair_total + 1);
+  int2 ids0[NPT];
 #pragma unroll
-  for (int k = 0; k < NPT; ++k) have[k] = false;
+  for (int k = 0; k < NPT; ++k)
+    ids0[k] = has[k] && cnt ? p.tab.ids[n0 + k * zstride] : make_int2(0, 0);
+  if (cnt == 0 || !inside) return;
+  if (tot0 > (unsigned long long)p.list_cap || tot1 > (unsigned long long)p.sf_cap) return;
+  const int4* __restrict__ lrec = p.lrec + 3 * (long long)coff;
+  Apply32 st[NPT];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) st[k].init(ids0[k]);
+  bool touched[NPT];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) touched[k] = false;
   for (int t = 0; t < cnt; ++t) {
-    const int4 A = lrec[3 * t];
+    const int4 A = __ldg(lrec + 3 * t);
     const unsigned ax = (unsigned)A.x, ay = (unsigned)A.y, az = (unsigned)A.z;
     const int lo0 = (int)(ax & 0xFFFFu), lo1 = (int)(ay & 0xFFFFu), lo2 = (int)(az & 0xFFFFu);
     const int hi2 = (int)(az >> 16);
@@ -1020,7 +1028,8 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
       any = any || in[k];
     }
     if (!any) continue;
-    const int4 B = lrec[3 * t + 1];
+    const int4 B = __ldg(lrec + 3 * t + 1);
+    const int4 U = __ldg(lrec + 3 * t + 2);
     const unsigned bz = (unsigned)B.z;
     const int bx = (int)(bz & 0xFFFFu), by = (int)(bz >> 16);
     const long long off = (long long)(((unsigned long long)(unsigned)B.y << 32) |
@@ -1030,13 +1039,9 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
     unsigned short cd[NPT];
 #pragma unroll
     for (int k = 0; k < NPT; ++k)
-      cd[k] = in[k] ? p.sfcode[off + (sz0 + k * dz - lo2) * plane] : (unsigned short)0;
+      cd[k] = in[k] ? __ldg(p.sfcode + off + (sz0 + k * dz - lo2) * plane) : (unsigned short)0;
 #pragma unroll
-    for (int k = 0; k < NPT; ++k)
-      if (in[k] && !have[k]) {
-        st[k].init(p.tab.ids[n0 + k * zstride]);
-        have[k] = true;
-      }
+    for (int k = 0; k < NPT; ++k) touched[k] = touched[k] || in[k];
     if (B.w) {
       const int hi = sx + g.off[0], hj = sy + g.off[1];
 #pragma unroll
@@ -1044,10 +1049,9 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
         if (!in[k]) continue;
         const int z = sz0 + k * dz;
         const int hk = z - box_of_z(g, z) * g.bz + g.off[2];  // z in the box's own frame
-        st[k].image(p, n0 + k * zstride, A.w, cd[k], spin_velocity(p.img[lrec[3 * t + 2].w], hi, hj, hk));
+        st[k].image(p, n0 + k * zstride, A.w, cd[k], spin_velocity(p.img[U.w], hi, hj, hk));
       }
     } else {
-      const int4 U = lrec[3 * t + 2];
       const float4 nv = make_float4(0.f, __int_as_float(U.x), __int_as_float(U.y),
                                     __int_as_float(U.z));
 #pragma unroll
@@ -1057,7 +1061,7 @@ __global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p)
   }
 #pragma unroll
   for (int k = 0; k < NPT; ++k)
-    if (have[k]) st[k].store(p, n0 + k * zstride);
+    if (touched[k]) st[k].store(p, n0 + k * zstride);
 }
 
 // img_prep; then two independent chains: the cell lists (scan, fill, sort)
@@ -1131,12 +1135,16 @@ static __device__ __forceinline__ void block_reduce_store(double (&acc)[12], con
     const int k = threadIdx.x;
     double sum = 0.0;
     for (int w = 0; w < RED_THREADS / 32; ++w) sum += part[w][k];
-    if (k < 3)
+    if (k < 3) {
       p.fh[3 * ip + k] = sum;
-    else if (k < 6)
+      if (p.fh2) p.fh2[3 * ip + k] = sum;
+    } else if (k < 6) {
       p.th[3 * ip + (k - 3)] = sum;
-    else
+      if (p.th2) p.th2[3 * ip + (k - 3)] = sum;
+    } else {
       p.S[6 * ip + (k - 6)] = -sum;
+      if (p.S2) p.S2[6 * ip + (k - 6)] = -sum;
+    }
   }
 }
 
@@ -1356,12 +1364,19 @@ __global__ void __launch_bounds__(RED_THREADS, 4) reduce_f32_kernel(ReduceParams
       sl = sl + part_lo[w][q] + e;
     }
     const double sum = (double)sh + (double)sl;
-    if (q < 3)
-      p.fh[3 * ip + q] = sum * p.box[bx.bidx].forceFactor;
-    else if (q < 6)
-      p.th[3 * ip + (q - 3)] = sum * p.box[bx.bidx].torqueFactor;
-    else
-      p.S[6 * ip + (q - 6)] = -(sum * p.box[bx.bidx].torqueFactor);
+    if (q < 3) {
+      const double v = sum * p.box[bx.bidx].forceFactor;
+      p.fh[3 * ip + q] = v;
+      if (p.fh2) p.fh2[3 * ip + q] = v;
+    } else if (q < 6) {
+      const double v = sum * p.box[bx.bidx].torqueFactor;
+      p.th[3 * ip + (q - 3)] = v;
+      if (p.th2) p.th2[3 * ip + (q - 3)] = v;
+    } else {
+      const double v = -(sum * p.box[bx.bidx].torqueFactor);
+      p.S[6 * ip + (q - 6)] = v;
+      if (p.S2) p.S2[6 * ip + (q - 6)] = v;
+    }
   }
 }
 
@@ -1371,6 +1386,38 @@ cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st) {
     reduce_f64_kernel<<<p.n, RED_THREADS, 0, st>>>(p);
   else
     reduce_f32_kernel<<<p.n, RED_THREADS, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+// One thread per image: the caller's image arrays into the handle's image
+// block (one launch instead of one copy per array).
+__global__ void gather_images_kernel(int n, const int* __restrict__ tag,
+                                     const double* __restrict__ x, const double* __restrict__ v,
+                                     const double* __restrict__ w, const double* __restrict__ r,
+                                     int* __restrict__ d_tag, double* __restrict__ d_xvw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const size_t nn = (size_t)n;
+  d_tag[i] = tag[i];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    d_xvw[3 * (size_t)i + c] = x[3 * (size_t)i + c];
+    d_xvw[3 * nn + 3 * (size_t)i + c] = v[3 * (size_t)i + c];
+    d_xvw[6 * nn + 3 * (size_t)i + c] = w[3 * (size_t)i + c];
+  }
+  d_xvw[9 * nn + i] = r[i];
+}
+
+const void* gather_images_fn() { return (const void*)gather_images_kernel; }
+const void* reduce_fn(int nodeF_is_double) {
+  return nodeF_is_double ? (const void*)reduce_f64_kernel : (const void*)reduce_f32_kernel;
+}
+
+cudaError_t launch_gather_images(int n, const int* tag, const double* x, const double* v,
+                                 const double* omega, const double* radius, int* d_tag,
+                                 double* d_xvw, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  gather_images_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, tag, x, v, omega, radius, d_tag, d_xvw);
   return cudaGetLastError();
 }
 

@@ -142,6 +142,48 @@ def test_step_device_matches_host_step():
     assert np.array_equal(S.cpu().numpy(), ha[2])
 
 
+def test_replayed_device_steps_take_each_calls_arrays():
+    """lbmpsm_step_device replays a captured graph once the image count has
+    held; every call's own input and output arrays must be the ones used.
+    Every step passes freshly allocated device buffers of moving, spinning
+    images; each step must equal the host-pointer step of the same images bit
+    for bit, in the caller's output buffers and in the handle's own."""
+    torch = pytest.importorskip("torch")
+    case = cases.CASES["shear_3d"]
+    tag, x, v, w, r = cases.initial_particles(case)
+    a = _lat(case, max_radius=float(np.max(r)) + 0.5)
+    b = _lat(case, max_radius=float(np.max(r)) + 0.5)
+    dev = torch.device("cuda", 0)
+    sets = []
+    for s in range(14):  # a ghost image leaves after step 3: the graph is captured anew
+        g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
+        sets.append(g)
+        x = cases.advance(case, x, v)
+    assert len({len(g["tag"]) for g in sets}) > 1
+    for s, g in enumerate(sets):
+        n = len(g["tag"])
+        ha = a.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+        a.apply_bc()
+        bb = {"out": [torch.full((n, 3), np.nan, dtype=torch.float64, device=dev),
+                      torch.full((n, 3), np.nan, dtype=torch.float64, device=dev),
+                      torch.full((n, 6), np.nan, dtype=torch.float64, device=dev)]}
+        for key in ("tag", "x", "v", "omega", "radius"):
+            bb[key] = torch.as_tensor(np.asarray(g[key], np.int32 if key == "tag" else np.float64),
+                                      device=dev)
+        torch.cuda.synchronize()
+        b.step_device(n, bb["tag"].data_ptr(), bb["x"].data_ptr(), bb["v"].data_ptr(),
+                      bb["omega"].data_ptr(), bb["radius"].data_ptr(),
+                      *[o.data_ptr() for o in bb["out"]])
+        b.apply_bc()
+        b.synchronize()
+        for got, exp in zip(bb["out"], ha):
+            assert np.array_equal(got.cpu().numpy(), exp), s
+        for got, exp in zip(b.read_forces(n), ha):
+            assert np.array_equal(got, exp), s
+    m = a.stored_mask()
+    assert np.array_equal(a.populations()[m], b.populations()[m])
+
+
 def test_fix_classes_drive_the_library(tmp_path):
     """The host mirror of the fixes runs the reference call order and writes VTI files."""
     from lbmpsm.host import Atoms, Domain, FixLbmPsm, FixLbmPsmBC, FixLbmPsmVTI, ghost_images
