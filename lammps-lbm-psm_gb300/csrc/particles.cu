@@ -407,7 +407,7 @@ static __device__ __forceinline__ int corner_count(int dim, float dxf, float dyf
   return -1;
 }
 
-constexpr int SFC_THREADS = 256;  // classification: one block per image
+constexpr int SFC_THREADS = 128;  // classification: one block per image
 constexpr int SFS_THREADS = 128;  // shell counting: persistent warps
 constexpr int SFS_BUF = 352;      // per-warp buffer of crossing rows (>= 32 + 32*10)
 
@@ -600,7 +600,10 @@ __global__ void __launch_bounds__(SFS_THREADS, 8) sf_shell_kernel(MapParams p) {
       }
       if (valid && amb) n = exact_count_2d(im, hx, hy);
     } else {
-      // axis order: outer a, middle b, inner c along the smallest |offset|
+      // axis order: inner c along the smallest |offset| (its rows run most
+      // nearly along the surface, so fewest cross it), outer a along the
+      // largest (the surface crosses the node nearly perpendicular to it, so
+      // fewest slabs are partial), middle b the other
       float da = dxf, db = dyf, dc = dzf;
       int pa = 0, pb = 1;
       {
@@ -609,6 +612,10 @@ __global__ void __launch_bounds__(SFS_THREADS, 8) sf_shell_kernel(MapParams p) {
           da = dyf; db = dzf; dc = dxf; pa = 1; pb = 2;
         } else if (ay <= ax && ay <= az) {
           da = dxf; db = dzf; dc = dyf; pa = 0; pb = 2;
+        }
+        if (fabsf(db) > fabsf(da)) {  // outer and middle swap: sums and margins are symmetric
+          const float t = da; da = db; db = t;
+          const int q = pa; pa = pb; pb = q;
         }
       }
       const float Ea = fabsf(da) + 2.0f, Eb = fabsf(db) + 2.0f, Ec = fabsf(dc) + 2.0f;
@@ -1105,7 +1112,7 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st, cudaStream_t aux, cu
 }
 
 // ------------------------------------------------------------------ reduce
-constexpr int RED_THREADS = 256;
+constexpr int RED_THREADS = 128;
 
 // Node (i, j, k) lies beyond the early-out radius rP of the image for
 // certain (FP32 distance with the margin proven for classify_node), so its
@@ -1215,10 +1222,11 @@ static __device__ __forceinline__ void two_sum(float a, float b, float& s, float
 // forces carry FP32 precision), accumulated per particle in double-float
 // (hi + lo pairs combined with TwoSum, ~48-bit significand) on the FP32 pipe,
 // then the per-warp results summed in FP64.  (FP64 arithmetic runs at 1/64 of
-// the FP32 rate on this GPU.)  Latency-bound: 64 registers (4 blocks per
-// multiprocessor) and two nodes' loads in flight per thread.
+// the FP32 rate on this GPU.)  Latency-bound: 64 registers, 128-thread blocks
+// (8 per multiprocessor: 2281 images of the 256^3 suspension fill the GPU in
+// finer waves than 256-thread blocks) and two nodes' loads in flight per thread.
 constexpr int RED_U = 2;
-__global__ void __launch_bounds__(RED_THREADS, 4) reduce_f32_kernel(ReduceParams p) {
+__global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams p) {
   const int ip = blockIdx.x;
   const Geom& g = p.g;
   const int tag = p.tag[ip];

@@ -65,6 +65,8 @@ def shell_count(dim, dxf, dyf, dzf, rsqf, D, r):
         da, db, dc, pa, pb = dyf, dzf, dxf, 1, 2
     elif ay <= ax and ay <= az:
         da, db, dc, pa, pb = dxf, dzf, dyf, 0, 2
+    if abs(db) > abs(da):  # the outer role takes the larger offset
+        da, db, pa, pb = db, da, pb, pa
     ea, eb, ec = abs(da) + F32(2), abs(db) + F32(2), abs(dc) + F32(2)
     m = F32(16) * U * (ea * ea + eb * eb + ec * ec + rsqf)
     lo, hi = rsqf - m, rsqf + m
