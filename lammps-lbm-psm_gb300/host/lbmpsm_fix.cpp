@@ -306,27 +306,40 @@ std::string FixLbmPsmVTI::write(long timestep, double u0) {
   if (lbmpsm_export_fields(h, useDouble_ ? 1 : 0, 1.0, fix_.get_rho(), u0, solid.data(),
                            rho.data(), u.data()) != LBMPSM_OK)
     lib_error(h);
-  const double dx = in.dx;
+  return write_vti_files(folder_, fileName_, timestep, dim, in.local, fix_.origin, in.dx, binary_,
+                         useDouble_, solid.data(), rho.data(), u.data());
+}
+
+std::string write_vti_files(const std::string& folder, const std::string& file_name, long timestep,
+                            int dim, const int local[3], const double origin[3], double dx,
+                            bool binary, bool use_double, const void* solid_p, const void* rho_p,
+                            const void* u_p) {
+  const long nx_i = local[0] - 2, ny_i = local[1] - 2, nz_i = dim == 3 ? local[2] - 2 : 1;
+  const size_t nP = (size_t)nx_i * ny_i * nz_i;
+  const size_t es = use_double ? 8 : 4;
+  const unsigned char* solid = static_cast<const unsigned char*>(solid_p);
+  const unsigned char* rho = static_cast<const unsigned char*>(rho_p);
+  const unsigned char* u = static_cast<const unsigned char*>(u_p);
   // coordinate of local node (1,1,1): origin + i*dx - dx (src/LBM_PSM_lattice.cpp:162-164)
-  const double* o = fix_.origin;
+  const double* o = origin;
   const double ox = o[0] + 1 * dx - dx * 1;
   const double oy = o[1] + 1 * dx - dx * 1;
   const double oz = dim == 3 ? o[2] + 1 * dx - dx * 1 : 0.0;
-  const std::string type = useDouble_ ? "Float64" : "Float32";
+  const std::string type = use_double ? "Float64" : "Float32";
   char stamp[32];
   std::snprintf(stamp, sizeof stamp, "%08ld", timestep);
-  const std::string base = fileName_ + "." + stamp;
-  const std::string vname = folder_ + "/" + base + "_rank0.vti";
+  const std::string base = file_name + "." + stamp;
+  const std::string vname = folder + "/" + base + "_rank0.vti";
   const std::string ext = "0 " + std::to_string(nx_i - 1) + " 0 " + std::to_string(ny_i - 1) +
                           " 0 " + std::to_string(nz_i - 1);
-  const std::string origin = fmt(ox) + " " + fmt(oy) + " " + fmt(oz);
+  const std::string org = fmt(ox) + " " + fmt(oy) + " " + fmt(oz);
   const std::string spacing = fmt(dx) + " " + fmt(dx) + " " + fmt(dx);
-  if (binary_) {
+  if (binary) {
     const uint32_t b_sz = (uint32_t)(nP * es), u_sz = (uint32_t)(3 * nP * es);
     std::ofstream f(vname, std::ios::binary);
     f << "<?xml version=\"1.0\"?>\n<VTKFile type=\"ImageData\" version=\"1.0\" "
          "byte_order=\"LittleEndian\" header_type=\"UInt32\">\n"
-      << " <ImageData WholeExtent=\"" << ext << "\" Origin=\"" << origin << "\" Spacing=\""
+      << " <ImageData WholeExtent=\"" << ext << "\" Origin=\"" << org << "\" Spacing=\""
       << spacing << "\">\n"
       << "  <Piece Extent=\"" << ext << "\">\n"
       << "   <PointData>\n"
@@ -337,9 +350,9 @@ std::string FixLbmPsmVTI::write(long timestep, double u0) {
       << "\" Name=\"Velocity\" NumberOfComponents=\"3\" format=\"appended\" offset=\""
       << 2 * (4 + (size_t)b_sz) << "\"/>\n"
       << "   </PointData>\n  </Piece>\n </ImageData>\n <AppendedData encoding=\"raw\">_";
-    auto put = [&](uint32_t sz, const std::vector<unsigned char>& d) {
+    auto put = [&](uint32_t sz, const unsigned char* d) {
       f.write(reinterpret_cast<const char*>(&sz), sizeof sz);
-      f.write(reinterpret_cast<const char*>(d.data()), (std::streamsize)d.size());
+      f.write(reinterpret_cast<const char*>(d), (std::streamsize)sz);
     };
     put(b_sz, solid);
     put(b_sz, rho);
@@ -348,37 +361,37 @@ std::string FixLbmPsmVTI::write(long timestep, double u0) {
   } else {
     std::ofstream f(vname);
     f << "<?xml version=\"1.0\"?>\n<VTKFile type=\"ImageData\" version=\"0.1\">\n"
-      << " <ImageData WholeExtent=\"" << ext << "\" Origin=\"" << origin << "\" Spacing=\""
+      << " <ImageData WholeExtent=\"" << ext << "\" Origin=\"" << org << "\" Spacing=\""
       << spacing << "\">\n"
       << "  <Piece Extent=\"" << ext << "\">\n   <PointData>\n";
-    auto value = [&](const std::vector<unsigned char>& d, size_t i) {
-      if (useDouble_) {
+    auto value = [&](const unsigned char* d, size_t i) {
+      if (use_double) {
         double x;
-        std::memcpy(&x, d.data() + 8 * i, 8);
+        std::memcpy(&x, d + 8 * i, 8);
         return x;
       }
       float x;
-      std::memcpy(&x, d.data() + 4 * i, 4);
+      std::memcpy(&x, d + 4 * i, 4);
       return (double)x;
     };
     struct Arr {
       const char* name;
       int comp;
-      const std::vector<unsigned char>* d;
+      const unsigned char* d;
     };
-    const Arr arrs[3] = {{"SolidFraction", 1, &solid}, {"Density", 1, &rho}, {"Velocity", 3, &u}};
+    const Arr arrs[3] = {{"SolidFraction", 1, solid}, {"Density", 1, rho}, {"Velocity", 3, u}};
     for (const Arr& ar : arrs) {
       f << "    <DataArray type=\"" << type << "\" Name=\"" << ar.name
         << "\" NumberOfComponents=\"" << ar.comp << "\" format=\"ascii\">\n";
       const size_t cnt = nP * (size_t)ar.comp;
-      for (size_t i = 0; i < cnt; ++i) f << fmt(value(*ar.d, i)) << (i % 10 == 9 ? "\n" : " ");
+      for (size_t i = 0; i < cnt; ++i) f << fmt(value(ar.d, i)) << (i % 10 == 9 ? "\n" : " ");
       f << "\n    </DataArray>\n";
     }
     f << "   </PointData>\n  </Piece>\n </ImageData>\n</VTKFile>";
   }
-  std::ofstream p(folder_ + "/" + base + ".pvti");
+  std::ofstream p(folder + "/" + base + ".pvti");
   p << "<?xml version=\"1.0\"?>\n<VTKFile type=\"PImageData\" version=\"0.1\">\n"
-    << " <PImageData WholeExtent=\"" << ext << "\" Origin=\"" << origin << "\" Spacing=\""
+    << " <PImageData WholeExtent=\"" << ext << "\" Origin=\"" << org << "\" Spacing=\""
     << spacing << "\">\n"
     << "  <PPointData>\n"
     << "   <PDataArray type=\"" << type << "\" Name=\"SolidFraction\"/>\n"

@@ -145,6 +145,17 @@ class FixLbmPsmRestart {
   std::string path_;
 };
 
+// The files of one `fix lbm-psm-vti` output step on one process
+// (src/fix_LBM_PSM_writeVTI.h:171-253): the .vti piece of the interior
+// nodes and the .pvti master file, for fields as lbmpsm_export_fields
+// returns them (float or double as use_double; solid and rho one value per
+// node, u three).  local: the local array sizes with the halo; origin: the
+// domain's boxlo.  Returns the piece's path.
+std::string write_vti_files(const std::string& folder, const std::string& file_name, long timestep,
+                            int dimension, const int local[3], const double origin[3], double dx,
+                            bool binary, bool use_double, const void* solid, const void* rho,
+                            const void* u);
+
 // the restart file of one rank: a uint32 count, then that many doubles
 std::string restart_file_name(int rank);
 void write_restart(const std::string& path, const std::vector<double>& f);

@@ -99,6 +99,14 @@ int orc_get_pdata(const orc_sim* s, int* ids, double* eps, double* us, double* F
 int orc_export_fields(const orc_sim* s, double B0, double rho0, double u0, double* solid,
                       double* rho, double* u);
 
+/* The file output of `fix lbm-psm-vti` on one process (vti_oracle.c, in the
+ * restatement library only): execute_write_vti<T>
+ * (src/fix_LBM_PSM_writeVTI.h:82-253) writing the piece and the master file
+ * for double fields solid, rho (one per interior node) and u (three). */
+int orc_write_vti(const char* folder, const char* name, int timestep, int binary, int use_double,
+                  int dimension, const int* local, const double* origin, double dx,
+                  const double* solid, const double* rho, const double* u);
+
 /* ---- LAMMPS single-rank emulation (not part of the reference sources) ----
  * Ghost images as CommBrick::borders() creates them on one process with
  * periodic axes: per dimension x,y,z, first the atoms with

@@ -224,6 +224,26 @@ def make_ghosts(dimension, boxlo, prd, periodic, cutghost, tag, x, v, omega, rad
                 radius=R[:n].copy(), owner=owner[:n].copy(), swap=swap[:n].copy(), nlocal=nloc)
 
 
+def write_vti(folder, name, timestep, binary, use_double, dimension, local, origin, dx, solid,
+              rho, u):
+    """The reference's VTI piece and PVTI master file for these fields (the C
+    restatement in vti_oracle.c; solid, rho one double per interior node, u
+    three)."""
+    lib = library("restatement")
+    fn = lib.orc_write_vti
+    fn.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _I, _D, C.c_double,
+                   _D, _D, _D]
+    loc = np.ascontiguousarray(local, dtype=np.int32)
+    org = np.ascontiguousarray(origin, dtype=np.float64)
+    solid = np.ascontiguousarray(solid, dtype=np.float64)
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    rc = fn(str(folder).encode(), name.encode(), int(timestep), int(binary), int(use_double),
+            int(dimension), _p(loc, _I), _p(org), float(dx), _p(solid), _p(rho), _p(u))
+    if rc != 0:
+        raise OSError("orc_write_vti failed")
+
+
 def reverse_comm(vals: np.ndarray, owner, swap, nlocal, kind="restatement") -> np.ndarray:
     lib = library(kind)
     vals = np.ascontiguousarray(vals, dtype=np.float64).copy()
