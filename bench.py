@@ -5,23 +5,26 @@ HBM roofline, FP32 storage against the plain FP64 path.
 Workload (the sheared dense suspension): D3Q19 256^3 lattice, x and z
 periodic, Zou-He moving walls in y (top +0.01, bottom -0.01 lattice units,
 `fix lbm-psm-bc shear`), tau = 0.65, 2000 spheres of diameter 12 lattice
-units placed by seeded random sequential addition (solid fraction ~0.108),
-zero particle velocities.  Synthetic data: no dataset is involved.  One
-"step" is one LBM coupling step: particle map, fused collide + stream,
-per-particle force/torque/stresslet reduction, and the wall boundary
-condition.  The particles stay in place (their motion is the host DEM's
-job), but the map is recomputed every step exactly as for moving particles.
+units placed by seeded random sequential addition (solid fraction ~0.108).
+Synthetic data: no dataset is involved.  One "step" is one LBM coupling
+step: particle map, fused collide + stream, per-particle force/torque/
+stresslet reduction, and the wall boundary condition.  The spheres move on
+every step (each on its own seeded closed loop of radius 0.1 lattice units,
+their ghost images with them), so every step maps new sub-cell positions,
+as the host DEM's motion would make it do.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line on rank 0.  `value` is measured with the particle
-images resident in HBM and the step sequence replayed as a CUDA graph;
+Prints one JSON line on rank 0.  `value` is measured with the images'
+positions resident in HBM (one set per step of the loops) and handed to
+lbmpsm_step_device each step, which the library replays as a CUDA graph;
 `e2e` runs the same steps through the host-pointer C-ABI call (images copied
-up from pinned memory and forces copied back every step; the library replays
-each such step as one CUDA graph).  The lattice
-(1.27 GB in FP32) is ~10x larger than L2, so no L2 flush is needed between
-steps.  `--impl reference` times the CPU oracle (the reference algorithm
-restated in C, FP64, all host cores) on the same workload.
+up from pinned memory and forces copied back every step, also one graph per
+step).  The lattice (1.27 GB in FP32) is ~10x larger than L2, so no L2 flush
+is needed between steps.  `--impl reference` times the CPU oracle (the
+reference algorithm restated in C, FP64, all host cores) on the same
+workload.  `--workload ensemble` and `--workload adjoint` time the batched
+boxes and the drag sensitivities.
 """
 from __future__ import annotations
 
@@ -673,7 +676,24 @@ def run_ensemble(args):
         e1.synchronize()
         clk.mark(t_a, time.monotonic())
     t = e0.elapsed_time(e1) / 1e3
+    launches = grp.collide_launches
+    # the collide alone: lattice-only steps (no images: the group's graph is
+    # the collide launch and nothing else), for the roofline
+    for e in sorted(ens):
+        en = ens[e][0]
+        z3 = np.zeros((0, 3))
+        en.step(np.zeros(0, np.int32), np.zeros(0, np.int32), z3, z3, z3, np.zeros(0))
+    grp.run_fixed(2)
+    torch.cuda.synchronize()
+    e0.record(st)
+    grp.run_fixed(K)
+    e1.record(st)
+    e1.synchronize()
+    t_col = e0.elapsed_time(e1) / 1e3 / K
     grp.close()
+    peak, peak_kind = measured_peak_gbs()
+    bpn = BYTES_PER_NODE[args.storage]
+    achieved = bpn * nodes / t_col / 1e9
     per_class = {str(e): {"boxes": len(classes[e]), "nodes": len(classes[e]) * e ** 3}
                  for e in sorted(classes)}
     for e in list(ens):
@@ -713,8 +733,16 @@ def run_ensemble(args):
                                "(seeded RSA)", "nodes": nodes, "storage": args.storage,
                    "classes": per_class,
                    "launch": "one ensemble per edge class; the classes stepped as one group: "
-                             "one CUDA graph launch per step for all boxes, classes as concurrent "
-                             "branches"},
+                             "one CUDA graph launch per step for all boxes; the classes' maps and "
+                             "reductions as concurrent branches around ONE collide launch for "
+                             "every box (unless LBMPSM_GROUP_FUSE=0)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "collide_multi_kernel (one launch for the boxes of every size)"
+                               if launches == 1 else "collide_pipe_kernel (one launch per edge class)",
+                     "algorithmic_bytes_per_node": bpn, "collide_ms": round(t_col * 1e3, 4),
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "collide_launches_per_step": launches,
         "accuracy": acc, "clocks": clk.summary(),
     }
 

@@ -276,7 +276,20 @@ int lbmpsm_export_fields_static(lbmpsm_handle* h, int as_double, double B0, doub
  * before its members. */
 typedef struct lbmpsm_group lbmpsm_group;
 int lbmpsm_group_create(lbmpsm_handle* const* handles, int count, lbmpsm_group** out);
+/* When every member is 3-D and periodic on every axis, the members share
+ * storage precision and PSM weighting, either all or none have a body force,
+ * there are at most 16 members and (FP32/FP16/BF16 storage) no x-row is longer
+ * than 128 nodes, the collide of all members is ONE persistent launch per
+ * step: its blocks walk tiles of one to several x-rows of every member (small
+ * boxes pack several rows per tile) and run each member's own node collision,
+ * so the results equal the members' own steps bit for bit.  The maps, faces
+ * and reductions of the members run as concurrent graph branches before and
+ * after it.  Otherwise each member keeps its own collide launch.  The
+ * environment variable LBMPSM_GROUP_FUSE=0 keeps the per-member launches. */
 int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps);
+/* Collide launches per step of the group's current graphs: 1 when fused,
+ * the member count otherwise, -1 before the first run. */
+int lbmpsm_group_collide_launches(const lbmpsm_group* g);
 void* lbmpsm_group_stream(lbmpsm_group* g); /* the cudaStream_t the group's graphs run on */
 const char* lbmpsm_group_last_error(const lbmpsm_group* g);
 void lbmpsm_group_destroy(lbmpsm_group* g);

@@ -407,7 +407,8 @@ Table box_table(const lbmpsm_handle* h) {
   return t;
 }
 
-int collide(lbmpsm_handle* h) {
+// the handle's collide parameters for its next step
+CollideParams collide_params(const lbmpsm_handle* h) {
   CollideParams p{};
   p.g = h->g;
   p.f = h->f;
@@ -424,6 +425,20 @@ int collide(lbmpsm_handle* h) {
   p.status = h->d_status;
   p.pipe = h->pipe;
   p.full_wait_limit = h->full_wait_limit;
+  return p;
+}
+
+// bookkeeping of a launched collide: the macro store is done, one step more
+void collide_done(lbmpsm_handle* h) {
+  if (h->macro_requested) {
+    h->macro_requested = false;
+    h->macro_valid = true;
+  }
+  h->t += 1;
+}
+
+int collide(lbmpsm_handle* h) {
+  const CollideParams p = collide_params(h);
   const int odd = (int)(h->t & 1);
   cudaError_t e;
   switch (h->opt.storage) {
@@ -433,11 +448,7 @@ int collide(lbmpsm_handle* h) {
     default: e = launch_collide_f16(p, odd, h->stream); break;
   }
   CUDA_TRY(h, e);
-  if (h->macro_requested) {
-    h->macro_requested = false;
-    h->macro_valid = true;
-  }
-  h->t += 1;
+  collide_done(h);
   return LBMPSM_OK;
 }
 
@@ -488,13 +499,15 @@ int maybe_tune(lbmpsm_handle* h) {
 
 // map -> collide -> reduce on device image arrays (internal buffers)
 int enqueue_bc(lbmpsm_handle* h, cudaStream_t st);
-
 // One coupling step (map, collide, reduce) on the handle's stream; with bc,
 // also the boundary faces after the collide.  The faces touch only the
 // populations, which neither the reduction nor the next step's map reads,
 // so with images the face kernel runs on the auxiliary stream beside the
 // reduction.
-int enqueue_step(lbmpsm_handle* h, int n, bool bc = false) {
+int enqueue_step(lbmpsm_handle* h, int n, bool bc = false);
+
+// The particle map of a step with n images (nothing without images).
+int enqueue_map(lbmpsm_handle* h, int n) {
   // image block layout: x | v | omega (3n each) | radius (n)
   const int* tag = h->d_tag;
   const double* x = h->d_xvw;
@@ -542,8 +555,14 @@ int enqueue_step(lbmpsm_handle* h, int n, bool bc = false) {
     m.write32 = h->opt.storage != LBMPSM_STORAGE_FP64 ? 1 : 0;
     CUDA_TRY(h, launch_map(m, h->stream, h->aux, h->ev_fork, h->ev_join));
   }
-  int rc = collide(h);
-  if (rc) return rc;
+  return LBMPSM_OK;
+}
+
+// After the collide: the boundary faces (beside the reduction when there
+// are images) and the reduction.
+int enqueue_post(lbmpsm_handle* h, int n, bool bc) {
+  const int* tag = h->d_tag;
+  int rc = LBMPSM_OK;
   bool bc_aside = false;
   if (bc && !h->faces.empty()) {
     if (n > 0 && h->aux && h->ev_bc_fork && h->ev_bc_join) {
@@ -578,6 +597,13 @@ int enqueue_step(lbmpsm_handle* h, int n, bool bc = false) {
   if (bc_aside) CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->ev_bc_join, 0));
   h->last_n = n;
   return LBMPSM_OK;
+}
+
+int enqueue_step(lbmpsm_handle* h, int n, bool bc) {
+  int rc = enqueue_map(h, n);
+  if (!rc) rc = collide(h);
+  if (!rc) rc = enqueue_post(h, n, bc);
+  return rc;
 }
 
 int enqueue_bc(lbmpsm_handle* h, cudaStream_t st) {
@@ -1903,12 +1929,18 @@ struct lbmpsm_group {
   std::vector<lbmpsm_handle*> hs;
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t fork = nullptr, done = nullptr;
-  std::vector<cudaEvent_t> join;
+  cudaEvent_t fork = nullptr, done = nullptr, fork2 = nullptr;
+  std::vector<cudaEvent_t> join, join2;
   cudaGraphExec_t gexec[2]{nullptr, nullptr};
   std::vector<long long> gen;  // members' graph generations the graphs were captured at
   std::vector<int> cap_n, cap_bc;
   std::string err;
+  // one collide launch for every member (when they qualify): the member
+  // table in device memory and the launch shape
+  bool fused = false;
+  MultiMember* d_members = nullptr;
+  std::vector<MultiMember> members;
+  MultiCollide mc{};
 };
 
 namespace {
@@ -1929,6 +1961,50 @@ void group_drop(lbmpsm_group* g) {
       cudaGraphExecDestroy(g->gexec[k]);
       g->gexec[k] = nullptr;
     }
+}
+
+// Whether the members' collides run as one launch, and if so its member
+// table and shape.  The members must be 3-D and periodic on every axis,
+// share storage precision and PSM weighting, and either all have a body
+// force or none; at most MULTI_MAX members; the row pipeline takes rows of
+// up to 128 nodes.  LBMPSM_GROUP_FUSE=0 keeps one collide per member.
+int group_plan_collide(lbmpsm_group* g) {
+  g->fused = false;
+  const char* env = std::getenv("LBMPSM_GROUP_FUSE");
+  if (env && std::atoi(env) == 0) return LBMPSM_OK;
+  const size_t m = g->hs.size();
+  if (m > (size_t)MULTI_MAX || !g->d_members) return LBMPSM_OK;
+  const lbmpsm_handle* h0 = g->hs[0];
+  for (const lbmpsm_handle* h : g->hs) {
+    if (h->g.dim != 3 || h->opt.storage != h0->opt.storage ||
+        h->opt.psm_weighting != h0->opt.psm_weighting || h->any_force != h0->any_force)
+      return LBMPSM_OK;
+    for (int d = 0; d < 3; ++d)
+      if (!h->g.per[d]) return LBMPSM_OK;
+  }
+  g->members.assign(m, MultiMember{});
+  for (size_t i = 0; i < m; ++i) {
+    g->members[i].p = collide_params(g->hs[i]);
+    g->members[i].p.store_macro = 0;
+    g->members[i].has_force = g->hs[i]->any_force ? 1 : 0;
+  }
+  MultiCollide mc{};
+  mc.m = g->d_members;
+  mc.nm = (int)m;
+  mc.any_force = h0->any_force ? 1 : 0;
+  mc.status = g->hs[0]->d_status;
+  mc.full_wait_limit = g->hs[0]->full_wait_limit;
+  if (prepare_collide_multi(mc, g->members.data(), h0->opt.storage, h0->sm_count) != cudaSuccess) {
+    cudaGetLastError();
+    return LBMPSM_OK;  // (rows too wide, or too many tiles): one collide per member
+  }
+  // ordered after the group's earlier launches, which may still read the table
+  GROUP_TRY(g, cudaMemcpyAsync(g->d_members, g->members.data(), sizeof(MultiMember) * m,
+                               cudaMemcpyHostToDevice, g->stream));
+  GROUP_TRY(g, cudaStreamSynchronize(g->stream));
+  g->mc = mc;
+  g->fused = true;
+  return LBMPSM_OK;
 }
 }  // namespace
 
@@ -1951,11 +2027,15 @@ int lbmpsm_group_create(lbmpsm_handle* const* handles, int count, lbmpsm_group**
   g->hs.assign(handles, handles + count);
   g->device = handles[0]->device;
   g->join.assign((size_t)count, nullptr);
+  g->join2.assign((size_t)count, nullptr);
   bool ok = cudaSetDevice(g->device) == cudaSuccess &&
             cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&g->fork2, cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming) == cudaSuccess;
   for (auto& e : g->join) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  for (auto& e : g->join2) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaMalloc(&g->d_members, sizeof(MultiMember) * MULTI_MAX) == cudaSuccess;
   if (!ok) {
     lbmpsm_group_destroy(g);
     return fail(nullptr, LBMPSM_ERR_CUDA, "group set-up failed");
@@ -1971,6 +2051,10 @@ void lbmpsm_group_destroy(lbmpsm_group* g) {
   group_drop(g);
   for (auto e : g->join)
     if (e) cudaEventDestroy(e);
+  for (auto e : g->join2)
+    if (e) cudaEventDestroy(e);
+  if (g->fork2) cudaEventDestroy(g->fork2);
+  if (g->d_members) cudaFree(g->d_members);
   if (g->fork) cudaEventDestroy(g->fork);
   if (g->done) cudaEventDestroy(g->done);
   if (g->stream) cudaStreamDestroy(g->stream);
@@ -1980,6 +2064,11 @@ void lbmpsm_group_destroy(lbmpsm_group* g) {
 const char* lbmpsm_group_last_error(const lbmpsm_group* g) { return g ? g->err.c_str() : ""; }
 
 void* lbmpsm_group_stream(lbmpsm_group* g) { return g ? (void*)g->stream : nullptr; }
+
+int lbmpsm_group_collide_launches(const lbmpsm_group* g) {
+  if (!g || (!g->gexec[0] && !g->gexec[1])) return -1;
+  return g->fused ? 1 : (int)g->hs.size();
+}
 
 int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps) {
   if (!g || nsteps < 0) return LBMPSM_ERR_ARG;
@@ -2014,17 +2103,51 @@ int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps) {
       cudaGraph_t graph = nullptr;
       std::vector<long long> t0(m);
       for (size_t i = 0; i < m; ++i) t0[i] = g->hs[i]->t;
+      if (!g->gexec[par ^ 1]) {  // planned once for both parities' graphs
+        const int prc = group_plan_collide(g);
+        if (prc) return prc;
+      }
       GROUP_TRY(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
       int rc = LBMPSM_OK;
       cudaError_t ce = cudaEventRecord(g->fork, g->stream);
-      for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
-        lbmpsm_handle* h = g->hs[i];
-        ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
-        if (ce != cudaSuccess) break;
-        rc = enqueue_step(h, h->last_n, true);
-        if (rc) rc = gfail(g, rc, h->err);
-        if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
-        if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
+      if (!g->fused) {
+        // each member's whole step as one branch
+        for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
+          lbmpsm_handle* h = g->hs[i];
+          ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
+          if (ce != cudaSuccess) break;
+          rc = enqueue_step(h, h->last_n, true);
+          if (rc) rc = gfail(g, rc, h->err);
+          if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
+          if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
+        }
+      } else {
+        // the members' maps as branches, one collide launch for all members,
+        // then their boundary faces and reductions as branches
+        for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
+          lbmpsm_handle* h = g->hs[i];
+          ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
+          if (ce != cudaSuccess) break;
+          rc = enqueue_map(h, h->last_n);
+          if (rc) rc = gfail(g, rc, h->err);
+          if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
+          if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
+        }
+        if (!rc && ce == cudaSuccess)
+          ce = launch_collide_multi(g->mc, g->hs[0]->opt.storage, par, g->stream);
+        if (!rc && ce == cudaSuccess) {
+          for (size_t i = 0; i < m; ++i) collide_done(g->hs[i]);
+          ce = cudaEventRecord(g->fork2, g->stream);
+        }
+        for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
+          lbmpsm_handle* h = g->hs[i];
+          ce = cudaStreamWaitEvent(h->stream, g->fork2, 0);
+          if (ce != cudaSuccess) break;
+          rc = enqueue_post(h, h->last_n, true);
+          if (rc) rc = gfail(g, rc, h->err);
+          if (!rc) ce = cudaEventRecord(g->join2[i], h->stream);
+          if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join2[i], 0);
+        }
       }
       cudaError_t ee = cudaStreamEndCapture(g->stream, &graph);
       for (size_t i = 0; i < m; ++i) g->hs[i]->t = t0[i];  // captured, not run

@@ -123,17 +123,11 @@ struct CollideUnroll<L, L::Q> {
                                              PsmNode&) {}
 };
 
+// One node of the FP64 collide + A-A stream step.
 template <class L, bool ODD>
-__global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
+__device__ __forceinline__ void collide_f64_node(const CollideParams& p, int sx, int sy, int sz) {
   constexpr int Q = L::Q;
   const Geom& g = p.g;
-  // blocks: (row, x-chunk) folded into blockIdx.x (rows can exceed the 65535 limit of y)
-  const int xblocks = (g.S[0] + blockDim.x - 1) / blockDim.x;
-  const int row = blockIdx.x / xblocks;
-  const int sx = (blockIdx.x - row * xblocks) * blockDim.x + threadIdx.x;
-  if (sx >= g.S[0]) return;
-  const int sy = row % g.S[1];
-  const int sz = row / g.S[1];
   const long long n = node_index(g, sx, sy, sz);
   const Nbr nb = make_nbr(g, sx, sy, sz);
   const BoxParams bp = p.box[box_of_z(g, sz)];  // copied: read once, before any store
@@ -246,6 +240,48 @@ __global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
       if (nbr_ok(nb, cx, cy, cz)) F[q * Np + n + nbr_off(nb, cx, cy, cz)] = f[q];
     }
   }
+}
+
+template <class L, bool ODD>
+__global__ void __launch_bounds__(128) collide_f64_kernel(CollideParams p) {
+  const Geom& g = p.g;
+  // blocks: (row, x-chunk) folded into blockIdx.x (rows can exceed the 65535 limit of y)
+  const int xblocks = (g.S[0] + blockDim.x - 1) / blockDim.x;
+  const int row = blockIdx.x / xblocks;
+  const int sx = (blockIdx.x - row * xblocks) * blockDim.x + threadIdx.x;
+  if (sx >= g.S[0]) return;
+  const int sy = row % g.S[1];
+  const int sz = row / g.S[1];
+  collide_f64_node<L, ODD>(p, sx, sy, sz);
+}
+
+// The members of a group in one launch: member m owns blocks
+// [first[m], first[m+1]), laid out as its own kernel's (row, x-chunk) blocks;
+// every node runs the same code as above, so the results are the members'.
+template <class L, bool ODD>
+__global__ void __launch_bounds__(128) collide_f64_multi_kernel(MultiCollide mc) {
+  const int b = blockIdx.x;
+  int m = 0;
+  while (m + 1 < mc.nm && b >= mc.first[m + 1]) ++m;
+  const CollideParams& p = mc.m[m].p;
+  const Geom& g = p.g;
+  const int S0 = g.S[0], S1 = g.S[1];
+  const int xblocks = (S0 + blockDim.x - 1) / blockDim.x;
+  const int lb = b - mc.first[m];
+  const int row = lb / xblocks;
+  const int sx = (lb - row * xblocks) * blockDim.x + threadIdx.x;
+  if (sx >= S0) return;
+  collide_f64_node<L, ODD>(p, sx, row % S1, row / S1);
+}
+
+cudaError_t launch_collide_f64_multi(const MultiCollide& mc, int odd, cudaStream_t st) {
+  const unsigned grid = (unsigned)mc.first[mc.nm];
+  if (grid == 0) return cudaSuccess;
+  if (odd)
+    collide_f64_multi_kernel<D3Q19, true><<<grid, 128, 0, st>>>(mc);
+  else
+    collide_f64_multi_kernel<D3Q19, false><<<grid, 128, 0, st>>>(mc);
+  return cudaGetLastError();
 }
 
 template <class L>

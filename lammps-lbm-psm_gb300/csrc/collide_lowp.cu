@@ -590,6 +590,332 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
   }
 }
 
+// The kernel's dynamic shared-memory limit is a property of the kernel, not
+// of a launch: lattices of different row lengths share it, so it is only ever
+// raised (a lattice set up later with shorter rows must not lower the limit
+// that an earlier one launches with).
+static cudaError_t raise_smem_limit(const void* fn, size_t smem) {
+  cudaFuncAttributes a{};
+  cudaError_t e = cudaFuncGetAttributes(&a, fn);
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= smem) return cudaSuccess;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// ------------------------------------------------------ several lattices
+// The row pipeline above over the members of a group in one persistent
+// launch.  The work is a list of tiles: member m owns tiles
+// [first[m], first[m+1]); a tile is k consecutive x-rows of one storage
+// plane of the member (rows y0 .. y0+k-1, fewer at the plane's end), k chosen
+// per member so that k rows fill the consumers (boxes of edge 32 take three
+// rows per tile, 48 two, 64-96 one).  Block b takes tiles b, b + G, ...; the
+// producer lane q moves direction q of each of the tile's rows with one bulk
+// copy per row, the consumers take one node each (thread t: row t / S0,
+// x = t % S0) and run the members' own node collision, so the results are
+// those of the members' own launches.  Every member is periodic on every axis
+// (rows and their neighbour rows always exist), and either every member has a
+// body force or none has.  The waits are bounded as in the single-lattice
+// kernel.
+struct TileRef {
+  int m, z, y0, k;
+};
+__device__ __forceinline__ TileRef tile_of(const MultiCollide& mc, int t) {
+  int m = 0;
+  while (m + 1 < mc.nm && t >= mc.first[m + 1]) ++m;
+  const MultiMember& mm = mc.m[m];
+  const unsigned lt = (unsigned)(t - mc.first[m]);
+  const int z = (int)fast_div(lt, mm.ftpp);
+  TileRef r;
+  r.m = m;
+  r.z = z;
+  r.y0 = ((int)lt - z * mm.tpp) * mm.k;
+  const int rest = mm.p.g.S[1] - r.y0;
+  r.k = rest < mm.k ? rest : mm.k;
+  return r;
+}
+
+constexpr int MULTI_MAX_ROW = 128;  // the widest row (nodes) a fused launch takes
+
+template <class L, typename T, bool ODD, bool FORCE, int NST>
+__global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 4) collide_multi_kernel(MultiCollide mc) {
+  static_assert(NST >= 2, "stages");
+  constexpr int Q = L::Q;
+  static_assert(Q <= 32, "one producer lane per direction");
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long full[NST], done[NST];
+  __shared__ int s_abort;
+  const int G = gridDim.x;
+  const int ncons = (int)blockDim.x - 32;
+  const int tcp = mc.tcp;
+  const unsigned stage_bytes = (unsigned)(Q * tcp * (int)sizeof(T));
+  const unsigned smem0 = smem_addr(smem_raw);
+  const int tid = threadIdx.x;
+  const int ntiles = mc.first[mc.nm];
+  const int K = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / G + 1 : 0;
+
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(smem_addr(&full[s]), 1);
+      mbar_init(smem_addr(&done[s]), (unsigned)ncons);
+    }
+    s_abort = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  if (tid >= ncons) {
+    // ------------------------------------------------------------ producer
+    const int lane = tid - ncons;
+    const bool mine = lane < Q;
+    int ey = 0, ez = 0, qo = 0;
+#pragma unroll
+    for (int qq = 0; qq < Q; ++qq)
+      if (qq == lane) {
+        ey = L::ey(qq);
+        ez = L::ez(qq);
+        qo = L::opp(qq);
+      }
+    int ls = 0, ss = 0, sph = 0;
+    int loaded = 0, stored = 0;
+    bool ok = true;
+    while (stored < K) {
+      const bool can_load = loaded < K && loaded - stored < NST;
+      if (!can_load) {
+        // store the oldest tile once the consumers are done with it
+        ok = __all_sync(0xffffffffu, mbar_wait_abortable(smem_addr(&done[ss]), sph, &s_abort));
+        if (!ok) break;
+        const TileRef tr = tile_of(mc, (int)blockIdx.x + stored * G);
+        if (mine) {
+          const CollideParams& p = mc.m[tr.m].p;
+          const Geom& g = p.g;
+          T* F = static_cast<T*>(p.f);
+          const unsigned row_bytes = (unsigned)(g.P0 * (int)sizeof(T));
+          for (int r = 0; r < tr.k; ++r) {
+            long long base = ((long long)tr.z * g.S[1] + tr.y0 + r) * g.P0;
+            if (ODD) row_of(g, tr.y0 + r, tr.z, ey, ez, base);
+            bulk_store(F + lane * g.Np + base,
+                       smem0 + ss * stage_bytes + (unsigned)((lane * tcp + r * g.P0) * (int)sizeof(T)),
+                       row_bytes);
+          }
+        }
+        bulk_commit();
+        ++stored;
+        if (++ss == NST) {
+          ss = 0;
+          sph ^= 1;
+        }
+        continue;
+      }
+      if (loaded >= NST) {
+        // the stage held the tile stored just before: wait until the store
+        // has read it (each lane its own bulk group)
+        bulk_wait_read0();
+        __syncwarp();
+      }
+      const TileRef tr = tile_of(mc, (int)blockIdx.x + loaded * G);
+      const CollideParams& p = mc.m[tr.m].p;
+      const Geom& g = p.g;
+      const unsigned row_bytes = (unsigned)(g.P0 * (int)sizeof(T));
+      const unsigned bar = smem_addr(&full[ls]);
+      if (lane == 0) mbar_expect_tx(bar, (unsigned)(Q * tr.k) * row_bytes);
+      __syncwarp();
+      if (mine) {
+        const T* F = static_cast<const T*>(p.f);
+        for (int r = 0; r < tr.k; ++r) {
+          long long base = ((long long)tr.z * g.S[1] + tr.y0 + r) * g.P0;
+          if (ODD) row_of(g, tr.y0 + r, tr.z, -ey, -ez, base);
+          bulk_load(smem0 + ls * stage_bytes + (unsigned)((lane * tcp + r * g.P0) * (int)sizeof(T)),
+                    F + (ODD ? qo : lane) * g.Np + base, row_bytes, bar);
+        }
+      }
+      ++loaded;
+      if (++ls == NST) ls = 0;
+    }
+    if (!ok) {
+      if (lane == 0) atomicOr(mc.status, STATUS_TIMEOUT);
+      // let the loads still in flight land: tiles stored .. loaded-1
+      int ts = ss, tph = sph;
+      for (int k = stored; k < loaded; ++k) {
+        mbar_wait_bounded(smem_addr(&full[ts]), tph);
+        if (++ts == NST) {
+          ts = 0;
+          tph ^= 1;
+        }
+      }
+    }
+    bulk_wait_all();
+    return;
+  }
+
+  // -------------------------------------------------------------- consumers
+  int s = 0, ph = 0;
+  for (int j = 0; j < K; ++j) {
+    const TileRef tr = tile_of(mc, (int)blockIdx.x + j * G);
+    const CollideParams& p = mc.m[tr.m].p;
+    const Geom& g = p.g;
+    const int S0 = g.S[0], P0 = g.P0;
+    const int r = tid / S0;
+    const int x = tid - r * S0;
+    const bool active = r < tr.k;
+    const int xm = x > 0 ? x - 1 : S0 - 1;
+    const int xp = x < S0 - 1 ? x + 1 : 0;
+    const float sc = p.scale16;
+    const long long n = ((long long)tr.z * g.S[1] + tr.y0 + r) * P0 + x;
+    uint8_t flag = 0;
+    float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r1;
+    if (active) {
+      flag = p.tab.flag[n];
+      if (flag) {
+        r1 = p.tab.rec32[2 * n];
+        r2 = p.tab.rec32[2 * n + 1];
+      }
+    }
+    bool ok = true;
+    if (tid == 0)
+      ok = mbar_wait_bounded(smem_addr(&full[s]), ph,
+                             mc.full_wait_limit > 0 ? mc.full_wait_limit
+                                                    : (mc.full_wait_limit < 0 ? 0 : MBAR_SPIN_LIMIT));
+    if (!named_bar_and(1, ncons, ok)) {
+      if (tid == 0) {
+        atomicOr(mc.status, STATUS_TIMEOUT);
+        *static_cast<volatile int*>(&s_abort) = 1;
+        __threadfence_block();
+      }
+      return;
+    }
+    T* buf = reinterpret_cast<T*>(smem_raw + (size_t)s * stage_bytes) + r * P0;
+    float f[Q];
+    if (active) {
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int ex = L::ex(q);
+        const int xs = ODD ? (ex == 0 ? x : (ex > 0 ? xm : xp)) : x;
+        f[q] = Store<T>::load(buf + q * tcp + xs, sc);
+      }
+      // every member has a body force, or none has (the host checks)
+      collide_node_lowp<L, FORCE>(f, p, p.box[box_of_z(g, tr.z)], n, flag, r1, r2);
+    }
+    // odd step: every input read before any output lands on a neighbour's
+    // column (the even step reads and writes only the thread's own column)
+    if (ODD) named_bar_sync(1, ncons);
+    if (active) {
+      if (!ODD) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) Store<T>::store(buf + L::opp(q) * tcp + x, f[q], sc);
+      } else {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int ex = L::ex(q);
+          const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
+          Store<T>::store(buf + q * tcp + xt, f[q], sc);
+        }
+      }
+    }
+    fence_async_smem();
+    mbar_arrive(smem_addr(&done[s]));
+    if (++s == NST) {
+      s = 0;
+      ph ^= 1;
+    }
+  }
+}
+
+constexpr int MULTI_STAGES = 3;
+
+template <typename T>
+static cudaError_t multi_prepare(MultiCollide& mc, MultiMember* mem, int sm_count) {
+  constexpr int Q = D3Q19::Q;
+  // consumers: the widest row, rounded up to whole warps
+  int smax = 0;
+  for (int m = 0; m < mc.nm; ++m) smax = std::max(smax, mem[m].p.g.S[0]);
+  if (smax < 1 || smax > MULTI_MAX_ROW) return cudaErrorInvalidValue;
+  const int tc = (smax + 31) / 32 * 32;
+  int tcp = 0, total = 0;
+  for (int m = 0; m < mc.nm; ++m) {
+    const Geom& g = mem[m].p.g;
+    int k = std::max(1, tc / g.S[0]);
+    k = std::min(k, g.S[1]);
+    mem[m].k = k;
+    mem[m].tpp = (g.S[1] + k - 1) / k;
+    mem[m].ftpp = make_fastdiv((unsigned)mem[m].tpp);
+    tcp = std::max(tcp, k * g.P0);
+    mc.first[m] = total;
+    const long long tiles = (long long)g.S[2] * mem[m].tpp;
+    // tile indices stay 32-bit and exact for the multiply-high division
+    if (tiles * mem[m].tpp >= (1ll << 32) || total + tiles >= (1ll << 31)) return cudaErrorInvalidValue;
+    total += (int)tiles;
+  }
+  mc.first[mc.nm] = total;
+  mc.tcp = (tcp + 7) / 8 * 8;
+  const int threads = tc + 32;
+  const size_t smem = (size_t)MULTI_STAGES * Q * mc.tcp * sizeof(T);
+  const void* fns[4] = {(const void*)collide_multi_kernel<D3Q19, T, false, false, MULTI_STAGES>,
+                        (const void*)collide_multi_kernel<D3Q19, T, false, true, MULTI_STAGES>,
+                        (const void*)collide_multi_kernel<D3Q19, T, true, false, MULTI_STAGES>,
+                        (const void*)collide_multi_kernel<D3Q19, T, true, true, MULTI_STAGES>};
+  cudaError_t e;
+  for (const void* fn : fns)
+    if ((e = raise_smem_limit(fn, smem)) != cudaSuccess) return e;
+  int per_sm = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[3], threads, smem)) !=
+      cudaSuccess)
+    return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  mc.pipe.stages = MULTI_STAGES;
+  mc.pipe.threads = threads;
+  mc.pipe.smem = smem;
+  mc.pipe.grid = (int)std::min<long long>(total, (long long)per_sm * sm_count);
+  return cudaSuccess;
+}
+
+cudaError_t prepare_collide_multi(MultiCollide& mc, MultiMember* mem, int storage, int sm_count) {
+  if (storage == 0) {
+    // FP64: the members' own (row, x-chunk) blocks in turn
+    int total = 0;
+    for (int m = 0; m < mc.nm; ++m) {
+      const Geom& g = mem[m].p.g;
+      const long long blocks = (long long)((g.S[0] + 127) / 128) * g.S[1] * g.S[2];
+      if (total + blocks >= (1ll << 31)) return cudaErrorInvalidValue;
+      mc.first[m] = total;
+      total += (int)blocks;
+    }
+    mc.first[mc.nm] = total;
+    return cudaSuccess;
+  }
+  if (storage == 1) return multi_prepare<float>(mc, mem, sm_count);
+  if (storage == 3) return multi_prepare<__nv_bfloat16>(mc, mem, sm_count);
+  return multi_prepare<__half>(mc, mem, sm_count);
+}
+
+template <typename T>
+static void launch_multi_t(const MultiCollide& mc, int odd, cudaStream_t st) {
+  const PipeConfig& c = mc.pipe;
+  if (odd) {
+    if (mc.any_force)
+      collide_multi_kernel<D3Q19, T, true, true, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+    else
+      collide_multi_kernel<D3Q19, T, true, false, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+  } else {
+    if (mc.any_force)
+      collide_multi_kernel<D3Q19, T, false, true, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+    else
+      collide_multi_kernel<D3Q19, T, false, false, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+  }
+}
+
+cudaError_t launch_collide_multi(const MultiCollide& mc, int storage, int odd, cudaStream_t st) {
+  if (storage == 0) return launch_collide_f64_multi(mc, odd, st);
+  if (mc.pipe.grid <= 0) return cudaSuccess;
+  if (storage == 1)
+    launch_multi_t<float>(mc, odd, st);
+  else if (storage == 3)
+    launch_multi_t<__nv_bfloat16>(mc, odd, st);
+  else
+    launch_multi_t<__half>(mc, odd, st);
+  return cudaGetLastError();
+}
+
 template <class L, typename T, int NST, int MINB>
 static cudaError_t pipe_prepare(const Geom& g, int sm_count, PipeConfig* cfg) {
   const int threads = (g.S[0] + 31) / 32 * 32 + 32;  // consumers + producer warp
@@ -600,9 +926,7 @@ static cudaError_t pipe_prepare(const Geom& g, int sm_count, PipeConfig* cfg) {
                         (const void*)collide_pipe_kernel<L, T, true, false, NST, MINB>,
                         (const void*)collide_pipe_kernel<L, T, true, true, NST, MINB>};
   for (const void* fn : fns)
-    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-      return e;
+    if ((e = raise_smem_limit(fn, smem)) != cudaSuccess) return e;
   int per_sm = 0;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[0], threads, smem)) !=
       cudaSuccess)

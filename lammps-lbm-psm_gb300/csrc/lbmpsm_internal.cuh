@@ -228,6 +228,32 @@ struct CollideParams {
 };
 
 
+// One collide launch over several lattices (the members of a group, e.g. one
+// batched ensemble per box size): the blocks take tiles of one member each.
+// The row pipeline (FP32 / FP16 / BF16) packs k consecutive x-rows of a
+// storage plane into a tile, so that small boxes fill the block's threads;
+// the FP64 kernel takes the members' (row, x-chunk) blocks in turn.  Members
+// must be 3-D and periodic on every axis.
+constexpr int MULTI_MAX = 16;
+struct MultiMember {
+  CollideParams p;  // the member's own collide parameters
+  int k;            // rows per tile (row pipeline)
+  int tpp;          // tiles per storage plane, ceil(S1 / k)
+  FastDiv ftpp;     // division by tpp
+  int has_force;    // the member has a body force (Guo terms)
+};
+struct MultiCollide {
+  const MultiMember* m;       // nm entries in device memory
+  int nm;
+  int first[MULTI_MAX + 1];   // first tile (row pipeline) or block (FP64) of each member;
+                              // first[nm] = total
+  int tcp;                    // row pipeline: stage capacity per direction (elements)
+  PipeConfig pipe;            // row pipeline: grid, threads, shared memory, stages
+  int any_force;
+  int* status;
+  long long full_wait_limit;  // as CollideParams
+};
+
 // Zou-He face list of one `fix lbm-psm-bc` keyword.
 enum FaceKind {
   FACE_VEL2_XN, FACE_VEL2_XP, FACE_DENS2_XP, FACE_VEL2_YN, FACE_VEL2_YP,
@@ -419,6 +445,12 @@ cudaError_t prepare_collide_lowp(const Geom& g, int storage, int sm_count, int s
 constexpr int LBMPSM_TUNE_CANDIDATES = 4;
 cudaError_t tune_collide_lowp(CollideParams p, int storage, int sm_count, cudaStream_t st,
                               PipeConfig* best, float* ms_out);
+// one launch over the members of mc (storage 0: FP64, 1: FP32, 2: FP16, 3: BF16);
+// prepare_collide_multi fills mc.first, tcp, pipe and the members' k / tpp
+// from their geometries (host copies in members) and the device's occupancy
+cudaError_t prepare_collide_multi(MultiCollide& mc, MultiMember* members, int storage, int sm_count);
+cudaError_t launch_collide_multi(const MultiCollide& mc, int storage, int odd, cudaStream_t st);
+cudaError_t launch_collide_f64_multi(const MultiCollide& mc, int odd, cudaStream_t st);
 cudaError_t launch_bc_f64(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f32(const BCParams& p, cudaStream_t st);
 cudaError_t launch_bc_f16(const BCParams& p, cudaStream_t st);

@@ -42,7 +42,7 @@ SYMBOLS = (
     "lbmpsm_create_batch", "lbmpsm_step_batch", "lbmpsm_select_box",
     "lbmpsm_adjoint_drag", "lbmpsm_tangent_drag",
     "lbmpsm_group_create", "lbmpsm_group_run_fixed", "lbmpsm_group_stream",
-    "lbmpsm_group_last_error", "lbmpsm_group_destroy",
+    "lbmpsm_group_last_error", "lbmpsm_group_destroy", "lbmpsm_group_collide_launches",
 )
 
 
@@ -140,6 +140,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.lbmpsm_group_last_error.restype = C.c_char_p
     lib.lbmpsm_group_destroy.argtypes = [H]
     lib.lbmpsm_group_destroy.restype = None
+    lib.lbmpsm_group_collide_launches.argtypes = [H]
     _lib = lib
     return lib
 
@@ -437,6 +438,11 @@ class Group:
     @property
     def stream(self) -> int:
         return self.lib.lbmpsm_group_stream(self.g)
+
+    @property
+    def collide_launches(self) -> int:
+        """Collide launches per step: 1 when the members' collides are fused."""
+        return int(self.lib.lbmpsm_group_collide_launches(self.g))
 
     def close(self):
         if getattr(self, "g", None):

@@ -173,3 +173,110 @@ def test_group_of_ensembles_of_different_sizes_equals_separate_runs():
         grp.run_fixed(1)
     assert e.value.code == lbmpsm.ERR_STATE
     grp.close()
+
+
+def _periodic_members(storage, edges=((24, 2), (16, 3), (10, 2)), seed=40):
+    """Ensembles of fully periodic boxes of several edges, every box with a
+    body force and spheres; the first step through the host call."""
+    members, nimg, specs = [], [], []
+    for e_i, (edge, nbox) in enumerate(edges):
+        boxes, imgs, bidx = [], [], []
+        for b in range(nbox):
+            tau = 0.62 + 0.11 * b + 0.05 * e_i
+            nu = (tau - 0.5) / 3.0
+            boxes.append(dict(dimension=3, boxlo=(0.5 * b, -0.25 * e_i, 0.0),
+                              prd=(float(edge),) * 3, periodic=(1, 1, 1), Nlc=9, lc=8.0,
+                              rho=1.0, nu=nu, Re=0.01 * 8 / nu, tau=tau,
+                              Fext=(1e-6 * (1 + b), 5e-7 * e_i, 0.0)))
+            rng = np.random.default_rng(seed + 10 * e_i + b)
+            lo = np.array(boxes[-1]["boxlo"])
+            x, r = cases.rsa(rng, 1 + b, (3.0, 4.5), lo, lo + edge, 3, min_gap=0.5)
+            n = len(x)
+            v = rng.normal(0, 0.01, (n, 3))
+            g = cases.product_make_ghosts(3, tuple(lo), boxes[-1]["prd"], (1, 1, 1), 5.5,
+                                          np.arange(1, n + 1), x, v, np.zeros((n, 3)), r)
+            imgs.append(g)
+            bidx.append(np.full(len(g["tag"]), b, np.int32))
+        cat = {k: np.concatenate([g[k] for g in imgs]) for k in ("tag", "x", "v", "omega", "radius")}
+        bi = np.concatenate(bidx)
+        ens = lbmpsm.Ensemble(boxes, storage=storage)
+        ens.step(bi, cat["tag"], cat["x"], cat["v"], cat["omega"], cat["radius"])
+        members.append(ens)
+        nimg.append(len(cat["tag"]))
+        specs.append((boxes, imgs))
+    return members, nimg, specs
+
+
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "fp16", "bf16"])
+def test_one_collide_launch_for_boxes_of_every_size(storage, monkeypatch):
+    """Periodic ensembles of edges 24, 16 and 10 (the row pipeline packs one,
+    two and three x-rows per tile) stepped as one group whose collide is a
+    single launch for all boxes: the same forces and populations, bit for
+    bit, as each ensemble stepped on its own and as the group with one
+    collide launch per member."""
+    solo, nimg, _ = _periodic_members(storage)
+    for m in solo:
+        m.run_fixed(7)
+    monkeypatch.setenv("LBMPSM_GROUP_FUSE", "0")
+    sep, _, _ = _periodic_members(storage)
+    g0 = lbmpsm.Group(sep)
+    g0.run_fixed(7)
+    assert g0.collide_launches == len(sep)
+    g0.close()
+    monkeypatch.delenv("LBMPSM_GROUP_FUSE")
+    fused, _, _ = _periodic_members(storage)
+    grp = lbmpsm.Group(fused)
+    assert grp.collide_launches == -1
+    grp.run_fixed(3)
+    assert grp.collide_launches == 1
+    grp.run_fixed(4)
+    grp.close()
+    for a, b, c, n in zip(solo, sep, fused, nimg):
+        assert a.steps == b.steps == c.steps == 8
+        fa = a.read_forces(n)
+        assert np.abs(fa[0]).max() > 0
+        for u, v_, w in zip(fa, b.read_forces(n), c.read_forces(n)):
+            assert np.array_equal(u, w) and np.array_equal(v_, w), storage
+        for box in range(a.nbox):
+            for e in (a, b, c):
+                e.select_box(box)
+            m = a.stored_mask()
+            pa = a.populations()[m]
+            assert np.array_equal(pa, b.populations()[m]), (storage, box)
+            assert np.array_equal(pa, c.populations()[m]), (storage, box)
+
+
+def test_fused_group_fp64_against_oracle_per_box():
+    """The batched workload against the CPU oracle: boxes of three edges, each
+    with its own tau, body force, origin and spheres, stepped as one fused
+    group in FP64; every box's per-image force, torque and stresslet within
+    1e-12 of a separate oracle lattice of that box, and its populations
+    within 1e-13 (spheres that cross a periodic seam are collided by the
+    reference on halo twins whose coordinates round differently)."""
+    import pyoracle
+    from test_parity_gpu import compare_fts
+    edges = ((14, 2), (12, 1), (10, 2))
+    members, nimg, specs = _periodic_members("fp64", edges=edges, seed=60)
+    steps = 9
+    grp = lbmpsm.Group(members)
+    grp.run_fixed(steps - 1)
+    assert grp.collide_launches == 1
+    grp.close()
+    for ens, n, (boxes, imgs) in zip(members, nimg, specs):
+        out = ens.read_forces(n)
+        k = 0
+        for b, (box, g) in enumerate(zip(boxes, imgs)):
+            orc = pyoracle.Sim("restatement", **box, bc_type=0)
+            a = (g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+            for _ in range(steps):
+                fo = orc.step(*a)
+            m = len(g["tag"])
+            got = tuple(o[k:k + m] for o in out)
+            k += m
+            assert compare_fts(got, fo, g["radius"]) <= 1e-12, (b, box["prd"])
+            ens.select_box(b)
+            mask = ens.stored_mask()
+            fg = ens.populations()[mask]
+            fr = orc.populations()[mask]
+            assert np.abs(fg - fr).max() <= 1e-13, (b, box["prd"])
+            orc.close()
