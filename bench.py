@@ -663,7 +663,7 @@ def run_ensemble(args):
     # every edge class is one ensemble; the group steps all of them as one
     # CUDA graph (one launch per step for all boxes)
     grp = lbmpsm.Group([ens[e][0] for e in sorted(ens)])
-    grp.run_fixed(W)
+    grp.run_fixed(max(W, 12))  # the group's tuner takes 8 of these steps
     st = torch.cuda.ExternalStream(grp.stream)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -677,6 +677,7 @@ def run_ensemble(args):
         clk.mark(t_a, time.monotonic())
     t = e0.elapsed_time(e1) / 1e3
     launches = grp.collide_launches
+    tune = grp.tune_ms
     # the collide alone: lattice-only steps (no images: the group's graph is
     # the collide launch and nothing else), for the roofline
     for e in sorted(ens):
@@ -743,6 +744,8 @@ def run_ensemble(args):
                      "algorithmic_bytes_per_node": bpn, "collide_ms": round(t_col * 1e3, 4),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
         "collide_launches_per_step": launches,
+        "group_tuner_ms_per_step": {"per_class_launches": round(tune[0], 4),
+                                    "one_launch": round(tune[1], 4)},
         "accuracy": acc, "clocks": clk.summary(),
     }
 

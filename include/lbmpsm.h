@@ -279,7 +279,7 @@ int lbmpsm_group_create(lbmpsm_handle* const* handles, int count, lbmpsm_group**
 /* When every member is 3-D and periodic on every axis, the members share
  * storage precision and PSM weighting, either all or none have a body force,
  * there are at most 16 members and (FP32/FP16/BF16 storage) no x-row is longer
- * than 128 nodes, the collide of all members is ONE persistent launch per
+ * than 96 nodes, the collide of all members is ONE persistent launch per
  * step: its blocks walk tiles of one to several x-rows of every member (small
  * boxes pack several rows per tile) and run each member's own node collision,
  * so the results equal the members' own steps bit for bit.  The maps, faces
@@ -290,6 +290,13 @@ int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps);
 /* Collide launches per step of the group's current graphs: 1 when fused,
  * the member count otherwise, -1 before the first run. */
 int lbmpsm_group_collide_launches(const lbmpsm_group* g);
+/* The group's tuner: the first lbmpsm_group_run_fixed call with at least 8
+ * steps, on members that qualify for one collide launch, runs two steps of
+ * each plan untimed (capturing their graphs) and two timed, then keeps the
+ * faster plan for the rest of the group's life (both give the same results
+ * bit for bit).  ms[0] = per-member launches, ms[1] = one launch, in ms per
+ * step (-1: not timed).  LBMPSM_GROUP_FUSE=0 / =1 fixes the plan instead. */
+int lbmpsm_group_tune_ms(const lbmpsm_group* g, float* ms);
 void* lbmpsm_group_stream(lbmpsm_group* g); /* the cudaStream_t the group's graphs run on */
 const char* lbmpsm_group_last_error(const lbmpsm_group* g);
 void lbmpsm_group_destroy(lbmpsm_group* g);

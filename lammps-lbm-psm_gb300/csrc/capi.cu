@@ -1941,6 +1941,14 @@ struct lbmpsm_group {
   MultiMember* d_members = nullptr;
   std::vector<MultiMember> members;
   MultiCollide mc{};
+  // which plan the graphs take: -1 = not yet timed (one launch when the
+  // members qualify), 0 = one collide per member, 1 = one launch for all;
+  // the group's tuner times both on live steps (their results are
+  // bit-identical) and keeps the faster
+  int plan_pref = -1;
+  bool tuned = false;
+  float tune_ms[2] = {-1.f, -1.f};  // ms per step: [0] per member, [1] one launch
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
 };
 
 namespace {
@@ -1968,20 +1976,29 @@ void group_drop(lbmpsm_group* g) {
 // share storage precision and PSM weighting, and either all have a body
 // force or none; at most MULTI_MAX members; the row pipeline takes rows of
 // up to 128 nodes.  LBMPSM_GROUP_FUSE=0 keeps one collide per member.
-int group_plan_collide(lbmpsm_group* g) {
-  g->fused = false;
-  const char* env = std::getenv("LBMPSM_GROUP_FUSE");
-  if (env && std::atoi(env) == 0) return LBMPSM_OK;
+// whether the members qualify for one collide launch
+bool group_fusable(const lbmpsm_group* g) {
   const size_t m = g->hs.size();
-  if (m > (size_t)MULTI_MAX || !g->d_members) return LBMPSM_OK;
+  if (m > (size_t)MULTI_MAX || !g->d_members) return false;
   const lbmpsm_handle* h0 = g->hs[0];
   for (const lbmpsm_handle* h : g->hs) {
     if (h->g.dim != 3 || h->opt.storage != h0->opt.storage ||
         h->opt.psm_weighting != h0->opt.psm_weighting || h->any_force != h0->any_force)
-      return LBMPSM_OK;
+      return false;
     for (int d = 0; d < 3; ++d)
-      if (!h->g.per[d]) return LBMPSM_OK;
+      if (!h->g.per[d]) return false;
   }
+  return true;
+}
+
+int group_plan_collide(lbmpsm_group* g) {
+  g->fused = false;
+  const char* env = std::getenv("LBMPSM_GROUP_FUSE");
+  if (env && std::atoi(env) == 0) return LBMPSM_OK;
+  if (g->plan_pref == 0 && !(env && std::atoi(env) == 1)) return LBMPSM_OK;
+  if (!group_fusable(g)) return LBMPSM_OK;
+  const size_t m = g->hs.size();
+  const lbmpsm_handle* h0 = g->hs[0];
   g->members.assign(m, MultiMember{});
   for (size_t i = 0; i < m; ++i) {
     g->members[i].p = collide_params(g->hs[i]);
@@ -2004,6 +2021,93 @@ int group_plan_collide(lbmpsm_group* g) {
   GROUP_TRY(g, cudaStreamSynchronize(g->stream));
   g->mc = mc;
   g->fused = true;
+  return LBMPSM_OK;
+}
+
+// Capture the graph of one step of every member for parity par.
+int group_capture(lbmpsm_group* g, int par) {
+  const size_t m = g->hs.size();
+  cudaGraph_t graph = nullptr;
+  std::vector<long long> t0(m);
+  for (size_t i = 0; i < m; ++i) t0[i] = g->hs[i]->t;
+  if (!g->gexec[par ^ 1]) {  // planned once for both parities' graphs
+    const int prc = group_plan_collide(g);
+    if (prc) return prc;
+  }
+  GROUP_TRY(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = LBMPSM_OK;
+  cudaError_t ce = cudaEventRecord(g->fork, g->stream);
+  if (!g->fused) {
+    // each member's whole step as one branch
+    for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
+      lbmpsm_handle* h = g->hs[i];
+      ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
+      if (ce != cudaSuccess) break;
+      rc = enqueue_step(h, h->last_n, true);
+      if (rc) rc = gfail(g, rc, h->err);
+      if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
+      if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
+    }
+  } else {
+    // the members' maps as branches, one collide launch for all members,
+    // then their boundary faces and reductions as branches
+    for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
+      lbmpsm_handle* h = g->hs[i];
+      ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
+      if (ce != cudaSuccess) break;
+      rc = enqueue_map(h, h->last_n);
+      if (rc) rc = gfail(g, rc, h->err);
+      if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
+      if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
+    }
+    if (!rc && ce == cudaSuccess)
+      ce = launch_collide_multi(g->mc, g->hs[0]->opt.storage, par, g->stream);
+    if (!rc && ce == cudaSuccess) {
+      for (size_t i = 0; i < m; ++i) collide_done(g->hs[i]);
+      ce = cudaEventRecord(g->fork2, g->stream);
+    }
+    for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
+      lbmpsm_handle* h = g->hs[i];
+      ce = cudaStreamWaitEvent(h->stream, g->fork2, 0);
+      if (ce != cudaSuccess) break;
+      rc = enqueue_post(h, h->last_n, true);
+      if (rc) rc = gfail(g, rc, h->err);
+      if (!rc) ce = cudaEventRecord(g->join2[i], h->stream);
+      if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join2[i], 0);
+    }
+  }
+  cudaError_t ee = cudaStreamEndCapture(g->stream, &graph);
+  for (size_t i = 0; i < m; ++i) g->hs[i]->t = t0[i];  // captured, not run
+  if (rc || ce != cudaSuccess || ee != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    if (rc) return rc;
+    GROUP_TRY(g, ce);
+    GROUP_TRY(g, ee);
+  }
+  cudaError_t ie = cudaGraphInstantiate(&g->gexec[par], graph, 0);
+  cudaGraphDestroy(graph);
+  GROUP_TRY(g, ie);
+  g->gen.resize(m);
+  g->cap_n.resize(m);
+  g->cap_bc.resize(m);
+  for (size_t i = 0; i < m; ++i) {
+    g->gen[i] = g->hs[i]->graph_gen;
+    g->cap_n[i] = g->hs[i]->last_n;
+    g->cap_bc[i] = g->hs[i]->faces.empty() ? 0 : 1;
+  }
+  return LBMPSM_OK;
+}
+
+// One step of the group: its graph for the members' parity (captured on
+// first use), launched on the group's stream.
+int group_step(lbmpsm_group* g) {
+  const int par = (int)(g->hs[0]->t & 1);
+  if (!g->gexec[par]) {
+    const int rc = group_capture(g, par);
+    if (rc) return rc;
+  }
+  GROUP_TRY(g, cudaGraphLaunch(g->gexec[par], g->stream));
+  for (lbmpsm_handle* h : g->hs) h->t += 1;
   return LBMPSM_OK;
 }
 }  // namespace
@@ -2036,6 +2140,7 @@ int lbmpsm_group_create(lbmpsm_handle* const* handles, int count, lbmpsm_group**
   for (auto& e : g->join) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
   for (auto& e : g->join2) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
   ok = ok && cudaMalloc(&g->d_members, sizeof(MultiMember) * MULTI_MAX) == cudaSuccess;
+  ok = ok && cudaEventCreate(&g->t0) == cudaSuccess && cudaEventCreate(&g->t1) == cudaSuccess;
   if (!ok) {
     lbmpsm_group_destroy(g);
     return fail(nullptr, LBMPSM_ERR_CUDA, "group set-up failed");
@@ -2054,6 +2159,8 @@ void lbmpsm_group_destroy(lbmpsm_group* g) {
   for (auto e : g->join2)
     if (e) cudaEventDestroy(e);
   if (g->fork2) cudaEventDestroy(g->fork2);
+  if (g->t0) cudaEventDestroy(g->t0);
+  if (g->t1) cudaEventDestroy(g->t1);
   if (g->d_members) cudaFree(g->d_members);
   if (g->fork) cudaEventDestroy(g->fork);
   if (g->done) cudaEventDestroy(g->done);
@@ -2064,6 +2171,13 @@ void lbmpsm_group_destroy(lbmpsm_group* g) {
 const char* lbmpsm_group_last_error(const lbmpsm_group* g) { return g ? g->err.c_str() : ""; }
 
 void* lbmpsm_group_stream(lbmpsm_group* g) { return g ? (void*)g->stream : nullptr; }
+
+int lbmpsm_group_tune_ms(const lbmpsm_group* g, float* ms) {
+  if (!g || !ms) return LBMPSM_ERR_ARG;
+  ms[0] = g->tune_ms[0];
+  ms[1] = g->tune_ms[1];
+  return LBMPSM_OK;
+}
 
 int lbmpsm_group_collide_launches(const lbmpsm_group* g) {
   if (!g || (!g->gexec[0] && !g->gexec[1])) return -1;
@@ -2097,80 +2211,38 @@ int lbmpsm_group_run_fixed(lbmpsm_group* g, int nsteps) {
     GROUP_TRY(g, cudaEventRecord(g->join[i], g->hs[i]->stream));
     GROUP_TRY(g, cudaStreamWaitEvent(g->stream, g->join[i], 0));
   }
-  for (int s = 0; s < nsteps; ++s) {
-    const int par = (int)(g->hs[0]->t & 1);
-    if (!g->gexec[par]) {
-      cudaGraph_t graph = nullptr;
-      std::vector<long long> t0(m);
-      for (size_t i = 0; i < m; ++i) t0[i] = g->hs[i]->t;
-      if (!g->gexec[par ^ 1]) {  // planned once for both parities' graphs
-        const int prc = group_plan_collide(g);
-        if (prc) return prc;
-      }
-      GROUP_TRY(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
-      int rc = LBMPSM_OK;
-      cudaError_t ce = cudaEventRecord(g->fork, g->stream);
-      if (!g->fused) {
-        // each member's whole step as one branch
-        for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
-          lbmpsm_handle* h = g->hs[i];
-          ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
-          if (ce != cudaSuccess) break;
-          rc = enqueue_step(h, h->last_n, true);
-          if (rc) rc = gfail(g, rc, h->err);
-          if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
-          if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
-        }
-      } else {
-        // the members' maps as branches, one collide launch for all members,
-        // then their boundary faces and reductions as branches
-        for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
-          lbmpsm_handle* h = g->hs[i];
-          ce = cudaStreamWaitEvent(h->stream, g->fork, 0);
-          if (ce != cudaSuccess) break;
-          rc = enqueue_map(h, h->last_n);
-          if (rc) rc = gfail(g, rc, h->err);
-          if (!rc) ce = cudaEventRecord(g->join[i], h->stream);
-          if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join[i], 0);
-        }
-        if (!rc && ce == cudaSuccess)
-          ce = launch_collide_multi(g->mc, g->hs[0]->opt.storage, par, g->stream);
-        if (!rc && ce == cudaSuccess) {
-          for (size_t i = 0; i < m; ++i) collide_done(g->hs[i]);
-          ce = cudaEventRecord(g->fork2, g->stream);
-        }
-        for (size_t i = 0; i < m && !rc && ce == cudaSuccess; ++i) {
-          lbmpsm_handle* h = g->hs[i];
-          ce = cudaStreamWaitEvent(h->stream, g->fork2, 0);
-          if (ce != cudaSuccess) break;
-          rc = enqueue_post(h, h->last_n, true);
-          if (rc) rc = gfail(g, rc, h->err);
-          if (!rc) ce = cudaEventRecord(g->join2[i], h->stream);
-          if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->join2[i], 0);
-        }
-      }
-      cudaError_t ee = cudaStreamEndCapture(g->stream, &graph);
-      for (size_t i = 0; i < m; ++i) g->hs[i]->t = t0[i];  // captured, not run
-      if (rc || ce != cudaSuccess || ee != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
+  // the group's tuner: with at least 8 steps to run and members that qualify
+  // for one collide launch, time two steps of each plan (after two untimed
+  // steps that capture its graphs) and keep the faster
+  const char* fenv = std::getenv("LBMPSM_GROUP_FUSE");
+  if (!g->tuned && nsteps >= 8 && !fenv && group_fusable(g)) {
+    g->tuned = true;
+    for (int plan = 1; plan >= 0; --plan) {
+      group_drop(g);
+      g->plan_pref = plan;
+      for (int k = 0; k < 2; ++k) {
+        const int rc = group_step(g);
         if (rc) return rc;
-        GROUP_TRY(g, ce);
-        GROUP_TRY(g, ee);
       }
-      cudaError_t ie = cudaGraphInstantiate(&g->gexec[par], graph, 0);
-      cudaGraphDestroy(graph);
-      GROUP_TRY(g, ie);
-      g->gen.resize(m);
-      g->cap_n.resize(m);
-      g->cap_bc.resize(m);
-      for (size_t i = 0; i < m; ++i) {
-        g->gen[i] = g->hs[i]->graph_gen;
-        g->cap_n[i] = g->hs[i]->last_n;
-        g->cap_bc[i] = g->hs[i]->faces.empty() ? 0 : 1;
+      GROUP_TRY(g, cudaEventRecord(g->t0, g->stream));
+      for (int k = 0; k < 2; ++k) {
+        const int rc = group_step(g);
+        if (rc) return rc;
       }
+      GROUP_TRY(g, cudaEventRecord(g->t1, g->stream));
+      GROUP_TRY(g, cudaEventSynchronize(g->t1));
+      float ms = 0.f;
+      GROUP_TRY(g, cudaEventElapsedTime(&ms, g->t0, g->t1));
+      g->tune_ms[plan] = ms / 2;
+      nsteps -= 4;
     }
-    GROUP_TRY(g, cudaGraphLaunch(g->gexec[par], g->stream));
-    for (size_t i = 0; i < m; ++i) g->hs[i]->t += 1;
+    const int best = g->tune_ms[1] <= g->tune_ms[0] ? 1 : 0;
+    if (best != g->plan_pref) group_drop(g);
+    g->plan_pref = best;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    const int rc = group_step(g);
+    if (rc) return rc;
   }
   // the members' later work is ordered after the group's
   GROUP_TRY(g, cudaEventRecord(g->done, g->stream));

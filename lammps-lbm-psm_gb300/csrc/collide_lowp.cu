@@ -15,6 +15,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "lbmpsm_internal.cuh"
 
@@ -74,7 +75,7 @@ __device__ __forceinline__ float edot(int cx, int cy, int cz, float vx, float vy
 // The warp takes the plain BGK loop when none of its nodes is a PSM node,
 // the one-slot loop when none holds two particles, else the two-slot loop;
 // an unused slot has B = 0 and leaves f' bit-identical to the shorter loop.
-template <class L, bool FORCE>
+template <class L, bool FORCE, bool MACRO = true>
 __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const CollideParams& p,
                                                   const BoxParams& bp, long long n, uint8_t flag,
                                                   float4 r1, float4 r2) {
@@ -96,7 +97,7 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
   const float rho = 1.0f + drho;
   const float inv = __frcp_rn(rho);
   const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-  if (p.store_macro) {
+  if (MACRO && p.store_macro) {
     p.rho_out[n] = 1.0 + (double)drho;
     p.u_out[3 * n + 0] = ux;
     p.u_out[3 * n + 1] = uy;
@@ -619,10 +620,10 @@ static cudaError_t raise_smem_limit(const void* fn, size_t smem) {
 struct TileRef {
   int m, z, y0, k;
 };
-__device__ __forceinline__ TileRef tile_of(const MultiCollide& mc, int t) {
+__device__ __forceinline__ TileRef tile_of(const MultiCollide& mc, const MultiMember* mem, int t) {
   int m = 0;
   while (m + 1 < mc.nm && t >= mc.first[m + 1]) ++m;
-  const MultiMember& mm = mc.m[m];
+  const MultiMember& mm = mem[m];
   const unsigned lt = (unsigned)(t - mc.first[m]);
   const int z = (int)fast_div(lt, mm.ftpp);
   TileRef r;
@@ -634,19 +635,31 @@ __device__ __forceinline__ TileRef tile_of(const MultiCollide& mc, int t) {
   return r;
 }
 
-constexpr int MULTI_MAX_ROW = 128;  // the widest row (nodes) a fused launch takes
+// the widest row (nodes) a fused launch takes; 128-thread blocks at eight per
+// multiprocessor (fewer registers, a few spilled to local memory, measured
+// faster than four to six blocks with none)
+constexpr int MULTI_MAX_ROW = 96;
 
 template <class L, typename T, bool ODD, bool FORCE, int NST>
-__global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 4) collide_multi_kernel(MultiCollide mc) {
+__global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 8) collide_multi_kernel(MultiCollide mc) {
   static_assert(NST >= 2, "stages");
   constexpr int Q = L::Q;
   static_assert(Q <= 32, "one producer lane per direction");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long full[NST], done[NST];
   __shared__ int s_abort;
+  // the member table in shared memory: every tile reads its member's
+  // parameters, which would otherwise be a chain of global loads per tile
+  __shared__ __align__(16) MultiMember s_mem[MULTI_MAX];
   const int G = gridDim.x;
   const int ncons = (int)blockDim.x - 32;
   const int tcp = mc.tcp;
+  {
+    const int words = mc.nm * (int)(sizeof(MultiMember) / sizeof(int));
+    const int* src = reinterpret_cast<const int*>(mc.m);
+    int* dst = reinterpret_cast<int*>(s_mem);
+    for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = __ldg(src + w);
+  }
   const unsigned stage_bytes = (unsigned)(Q * tcp * (int)sizeof(T));
   const unsigned smem0 = smem_addr(smem_raw);
   const int tid = threadIdx.x;
@@ -685,9 +698,9 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 4) collide_multi_kernel(Mu
         // store the oldest tile once the consumers are done with it
         ok = __all_sync(0xffffffffu, mbar_wait_abortable(smem_addr(&done[ss]), sph, &s_abort));
         if (!ok) break;
-        const TileRef tr = tile_of(mc, (int)blockIdx.x + stored * G);
+        const TileRef tr = tile_of(mc, s_mem, (int)blockIdx.x + stored * G);
         if (mine) {
-          const CollideParams& p = mc.m[tr.m].p;
+          const CollideParams& p = s_mem[tr.m].p;
           const Geom& g = p.g;
           T* F = static_cast<T*>(p.f);
           const unsigned row_bytes = (unsigned)(g.P0 * (int)sizeof(T));
@@ -713,8 +726,8 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 4) collide_multi_kernel(Mu
         bulk_wait_read0();
         __syncwarp();
       }
-      const TileRef tr = tile_of(mc, (int)blockIdx.x + loaded * G);
-      const CollideParams& p = mc.m[tr.m].p;
+      const TileRef tr = tile_of(mc, s_mem, (int)blockIdx.x + loaded * G);
+      const CollideParams& p = s_mem[tr.m].p;
       const Geom& g = p.g;
       const unsigned row_bytes = (unsigned)(g.P0 * (int)sizeof(T));
       const unsigned bar = smem_addr(&full[ls]);
@@ -751,8 +764,8 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 4) collide_multi_kernel(Mu
   // -------------------------------------------------------------- consumers
   int s = 0, ph = 0;
   for (int j = 0; j < K; ++j) {
-    const TileRef tr = tile_of(mc, (int)blockIdx.x + j * G);
-    const CollideParams& p = mc.m[tr.m].p;
+    const TileRef tr = tile_of(mc, s_mem, (int)blockIdx.x + j * G);
+    const CollideParams& p = s_mem[tr.m].p;
     const Geom& g = p.g;
     const int S0 = g.S[0], P0 = g.P0;
     const int r = tid / S0;
@@ -794,7 +807,7 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 4) collide_multi_kernel(Mu
         f[q] = Store<T>::load(buf + q * tcp + xs, sc);
       }
       // every member has a body force, or none has (the host checks)
-      collide_node_lowp<L, FORCE>(f, p, p.box[box_of_z(g, tr.z)], n, flag, r1, r2);
+      collide_node_lowp<L, FORCE, false>(f, p, p.box[box_of_z(g, tr.z)], n, flag, r1, r2);
     }
     // odd step: every input read before any output lands on a neighbour's
     // column (the even step reads and writes only the thread's own column)
@@ -821,16 +834,41 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 4) collide_multi_kernel(Mu
   }
 }
 
-constexpr int MULTI_STAGES = 3;
+constexpr int MULTI_STAGES = 3;  // stages of the fused launch (LBMPSM_MULTI_STAGES: 3-5)
+
+template <typename T, int NST>
+static cudaError_t multi_set_limits(size_t smem) {
+  const void* fns[4] = {(const void*)collide_multi_kernel<D3Q19, T, false, false, NST>,
+                        (const void*)collide_multi_kernel<D3Q19, T, false, true, NST>,
+                        (const void*)collide_multi_kernel<D3Q19, T, true, false, NST>,
+                        (const void*)collide_multi_kernel<D3Q19, T, true, true, NST>};
+  for (const void* fn : fns) {
+    const cudaError_t e = raise_smem_limit(fn, smem);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+static const void* multi_probe_fn(int nst) {
+  switch (nst) {
+    case 4: return (const void*)collide_multi_kernel<D3Q19, T, true, true, 4>;
+    case 5: return (const void*)collide_multi_kernel<D3Q19, T, true, true, 5>;
+    default: return (const void*)collide_multi_kernel<D3Q19, T, true, true, 3>;
+  }
+}
 
 template <typename T>
 static cudaError_t multi_prepare(MultiCollide& mc, MultiMember* mem, int sm_count) {
   constexpr int Q = D3Q19::Q;
-  // consumers: the widest row, rounded up to whole warps
+  // consumers: the widest row, rounded up to whole warps (LBMPSM_MULTI_CONSUMERS
+  // asks for more, up to MULTI_MAX_ROW, so that more rows share a tile)
   int smax = 0;
   for (int m = 0; m < mc.nm; ++m) smax = std::max(smax, mem[m].p.g.S[0]);
   if (smax < 1 || smax > MULTI_MAX_ROW) return cudaErrorInvalidValue;
-  const int tc = (smax + 31) / 32 * 32;
+  int tc = (smax + 31) / 32 * 32;
+  if (const char* env = std::getenv("LBMPSM_MULTI_CONSUMERS"))
+    tc = std::min(MULTI_MAX_ROW, std::max(tc, (std::atoi(env) + 31) / 32 * 32));
   int tcp = 0, total = 0;
   for (int m = 0; m < mc.nm; ++m) {
     const Geom& g = mem[m].p.g;
@@ -849,20 +887,19 @@ static cudaError_t multi_prepare(MultiCollide& mc, MultiMember* mem, int sm_coun
   mc.first[mc.nm] = total;
   mc.tcp = (tcp + 7) / 8 * 8;
   const int threads = tc + 32;
-  const size_t smem = (size_t)MULTI_STAGES * Q * mc.tcp * sizeof(T);
-  const void* fns[4] = {(const void*)collide_multi_kernel<D3Q19, T, false, false, MULTI_STAGES>,
-                        (const void*)collide_multi_kernel<D3Q19, T, false, true, MULTI_STAGES>,
-                        (const void*)collide_multi_kernel<D3Q19, T, true, false, MULTI_STAGES>,
-                        (const void*)collide_multi_kernel<D3Q19, T, true, true, MULTI_STAGES>};
-  cudaError_t e;
-  for (const void* fn : fns)
-    if ((e = raise_smem_limit(fn, smem)) != cudaSuccess) return e;
+  int nst = MULTI_STAGES;
+  if (const char* env = std::getenv("LBMPSM_MULTI_STAGES")) nst = std::atoi(env);
+  if (nst < 3 || nst > 5) nst = MULTI_STAGES;
+  const size_t smem = (size_t)nst * Q * mc.tcp * sizeof(T);
+  cudaError_t e = nst == 4 ? multi_set_limits<T, 4>(smem)
+                           : (nst == 5 ? multi_set_limits<T, 5>(smem) : multi_set_limits<T, 3>(smem));
+  if (e != cudaSuccess) return e;
   int per_sm = 0;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[3], threads, smem)) !=
-      cudaSuccess)
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, multi_probe_fn<T>(nst), threads,
+                                                         smem)) != cudaSuccess)
     return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  mc.pipe.stages = MULTI_STAGES;
+  mc.pipe.stages = nst;
   mc.pipe.threads = threads;
   mc.pipe.smem = smem;
   mc.pipe.grid = (int)std::min<long long>(total, (long long)per_sm * sm_count);
@@ -888,19 +925,28 @@ cudaError_t prepare_collide_multi(MultiCollide& mc, MultiMember* mem, int storag
   return multi_prepare<__half>(mc, mem, sm_count);
 }
 
-template <typename T>
-static void launch_multi_t(const MultiCollide& mc, int odd, cudaStream_t st) {
+template <typename T, int NST>
+static void launch_multi_n(const MultiCollide& mc, int odd, cudaStream_t st) {
   const PipeConfig& c = mc.pipe;
   if (odd) {
     if (mc.any_force)
-      collide_multi_kernel<D3Q19, T, true, true, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+      collide_multi_kernel<D3Q19, T, true, true, NST><<<c.grid, c.threads, c.smem, st>>>(mc);
     else
-      collide_multi_kernel<D3Q19, T, true, false, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+      collide_multi_kernel<D3Q19, T, true, false, NST><<<c.grid, c.threads, c.smem, st>>>(mc);
   } else {
     if (mc.any_force)
-      collide_multi_kernel<D3Q19, T, false, true, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+      collide_multi_kernel<D3Q19, T, false, true, NST><<<c.grid, c.threads, c.smem, st>>>(mc);
     else
-      collide_multi_kernel<D3Q19, T, false, false, MULTI_STAGES><<<c.grid, c.threads, c.smem, st>>>(mc);
+      collide_multi_kernel<D3Q19, T, false, false, NST><<<c.grid, c.threads, c.smem, st>>>(mc);
+  }
+}
+
+template <typename T>
+static void launch_multi_t(const MultiCollide& mc, int odd, cudaStream_t st) {
+  switch (mc.pipe.stages) {
+    case 4: launch_multi_n<T, 4>(mc, odd, st); break;
+    case 5: launch_multi_n<T, 5>(mc, odd, st); break;
+    default: launch_multi_n<T, 3>(mc, odd, st); break;
   }
 }
 

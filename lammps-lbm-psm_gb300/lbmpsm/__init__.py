@@ -43,6 +43,7 @@ SYMBOLS = (
     "lbmpsm_adjoint_drag", "lbmpsm_tangent_drag",
     "lbmpsm_group_create", "lbmpsm_group_run_fixed", "lbmpsm_group_stream",
     "lbmpsm_group_last_error", "lbmpsm_group_destroy", "lbmpsm_group_collide_launches",
+    "lbmpsm_group_tune_ms",
 )
 
 
@@ -141,6 +142,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.lbmpsm_group_destroy.argtypes = [H]
     lib.lbmpsm_group_destroy.restype = None
     lib.lbmpsm_group_collide_launches.argtypes = [H]
+    lib.lbmpsm_group_tune_ms.argtypes = [H, C.POINTER(C.c_float)]
     _lib = lib
     return lib
 
@@ -443,6 +445,15 @@ class Group:
     def collide_launches(self) -> int:
         """Collide launches per step: 1 when the members' collides are fused."""
         return int(self.lib.lbmpsm_group_collide_launches(self.g))
+
+    @property
+    def tune_ms(self):
+        """The tuner's ms per step: (per-member launches, one launch); -1 untimed."""
+        ms = (C.c_float * 2)()
+        rc = self.lib.lbmpsm_group_tune_ms(self.g, ms)
+        if rc != OK:
+            raise LbmPsmError(rc, self.lib.lbmpsm_group_last_error(self.g).decode())
+        return float(ms[0]), float(ms[1])
 
     def close(self):
         if getattr(self, "g", None):

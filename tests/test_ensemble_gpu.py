@@ -246,7 +246,7 @@ def test_one_collide_launch_for_boxes_of_every_size(storage, monkeypatch):
             assert np.array_equal(pa, c.populations()[m]), (storage, box)
 
 
-def test_fused_group_fp64_against_oracle_per_box():
+def test_fused_group_fp64_against_oracle_per_box(monkeypatch):
     """The batched workload against the CPU oracle: boxes of three edges, each
     with its own tau, body force, origin and spheres, stepped as one fused
     group in FP64; every box's per-image force, torque and stresslet within
@@ -255,6 +255,7 @@ def test_fused_group_fp64_against_oracle_per_box():
     reference on halo twins whose coordinates round differently)."""
     import pyoracle
     from test_parity_gpu import compare_fts
+    monkeypatch.setenv("LBMPSM_GROUP_FUSE", "1")  # the one-launch plan, whatever the tuner would pick
     edges = ((14, 2), (12, 1), (10, 2))
     members, nimg, specs = _periodic_members("fp64", edges=edges, seed=60)
     steps = 9
@@ -280,3 +281,29 @@ def test_fused_group_fp64_against_oracle_per_box():
             fr = orc.populations()[mask]
             assert np.abs(fg - fr).max() <= 1e-13, (b, box["prd"])
             orc.close()
+
+
+def test_group_tuner_keeps_the_results(monkeypatch):
+    """The group's tuner times both collide plans on live steps of the first
+    run of at least 8 steps and keeps the faster; the results stay those of
+    the members' own steps, bit for bit."""
+    monkeypatch.delenv("LBMPSM_GROUP_FUSE", raising=False)
+    solo, nimg, _ = _periodic_members("fp32", seed=80)
+    for m in solo:
+        m.run_fixed(11)
+    grouped, _, _ = _periodic_members("fp32", seed=80)
+    grp = lbmpsm.Group(grouped)
+    grp.run_fixed(11)
+    per_member, one = grp.tune_ms
+    assert per_member > 0 and one > 0
+    assert grp.collide_launches == (1 if one <= per_member else len(grouped))
+    grp.close()
+    for a, b, n in zip(solo, grouped, nimg):
+        assert a.steps == b.steps == 12
+        for u, w in zip(a.read_forces(n), b.read_forces(n)):
+            assert np.array_equal(u, w)
+        for box in range(a.nbox):
+            a.select_box(box)
+            b.select_box(box)
+            m = a.stored_mask()
+            assert np.array_equal(a.populations()[m], b.populations()[m])
