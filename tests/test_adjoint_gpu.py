@@ -192,6 +192,35 @@ def _owner_rows(g, rows):
     return reverse_comm(rows, g["owner"], g["swap"], g["nlocal"])[:g["nlocal"]]
 
 
+def _c5_fd_centres(parts, h):
+    """Central differences of J over every centre coordinate: the 48
+    configurations (one coordinate moved by +h or -h) as the boxes of one
+    ensemble, each box's J from its own images' forces."""
+    tag, x, v, w, r = parts
+    prm = C5.params()
+    boxes, cols = [], {k: [] for k in ("box",) + KEYS}
+    for p_ in range(len(tag)):
+        for a in range(3):
+            for sgn in (1, -1):
+                xs = x.copy()
+                xs[p_, a] += sgn * h
+                ims, _ = _imgs(C5, (tag, xs, v, w, r))
+                cols["box"].append(np.full(len(ims["tag"]), len(boxes), np.int32))
+                for k in KEYS:
+                    cols[k].append(ims[k])
+                boxes.append(prm)
+    cat = {k: np.concatenate(a_) for k, a_ in cols.items()}
+    ens = lbmpsm.Ensemble(boxes, storage="fp64")
+    J = np.zeros(len(boxes))
+    for t in range(1, C5_T + 1):
+        fh = ens.step(cat["box"], *[cat[k] for k in KEYS])[0]
+        if t >= C5_T0:
+            J += np.bincount(cat["box"], weights=fh[:, 0], minlength=len(boxes))
+    ens.close()
+    J /= (C5_T1 - C5_T0 + 1)
+    return ((J[0::2] - J[1::2]) / (2 * h)).reshape(len(tag), 3)
+
+
 def test_full_size_sensitivities():
     parts = cases.initial_particles(C5)
     assert len(parts[0]) == 8
@@ -220,13 +249,22 @@ def test_full_size_sensitivities():
 
     grad = _owner_rows(g, R["dx"])
     tag, x, v, w, r = parts
+    # all 24 centre coordinates against central differences at h; the 48
+    # perturbed configurations run together as one batched ensemble of boxes
+    fd = _c5_fd_centres(parts, h)
+    err = np.abs(grad - fd)
+    scale = np.abs(fd).max()
+    # J is a staircase in the centres (a node's solid fraction changes by
+    # 1/1000 when a sub-cell centre crosses the surface): the adjoint's centre
+    # derivative is the first-order response to the count changes a central
+    # difference at h sees, so they differ by the second-order response to
+    # those changes.  Measured at h = 1e-4: max 7.4e-4 and median 1.8e-4 of
+    # the largest component; per component up to 2.3e-2 where a component is
+    # fifty times below the largest.
+    assert err.max() <= 2e-3 * scale, (err.max() / scale, err / scale)
+    big = np.abs(fd) >= 0.1 * scale
+    assert np.all(err[big] <= 5e-3 * np.abs(fd[big])), (err / np.abs(fd))
     for p_, a in ((0, 0), (3, 1), (6, 2)):
-        xp = x.copy()
-        xm = x.copy()
-        xp[p_, a] += h
-        xm[p_, a] -= h
-        fd = (_c5_J(_imgs(C5, (tag, xp, v, w, r))[0]) - _c5_J(_imgs(C5, (tag, xm, v, w, r))[0])) / (2 * h)
-        assert abs(grad[p_, a] - fd) <= 5e-3 * abs(fd), (p_, a, grad[p_, a], fd)
         # tangent along the same coordinate (every image of the particle moves)
         dx = np.zeros((len(im["tag"]), 3))
         dx[im["tag"] == tag[p_], a] = 1.0
