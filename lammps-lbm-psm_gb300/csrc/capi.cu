@@ -40,7 +40,7 @@ struct lbmpsm_handle {
   cudaStream_t aux = nullptr;                  // cell-list kernels of the map
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_bc_fork = nullptr, ev_bc_join = nullptr;  // the BC beside the reduction
-  float scale16 = 4096.0f;
+  float scale16 = (float)(1 << FP16_SCALE_LOG2);
   // lattice
   void* f = nullptr;
   Table tab{};

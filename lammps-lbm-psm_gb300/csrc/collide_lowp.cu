@@ -21,29 +21,47 @@
 
 namespace lbmpsm {
 
+// load / store: deviations in FP32.  raw_load / raw_store: the stored value
+// times 2^-SH unscaled, i.e. the deviation times 2^SH, which the collide
+// kernels take as is (collide_node_lowp's SH).
 template <typename T>
 struct Store;
 template <>
 struct Store<float> {
+  static constexpr int SH = 0;
   __device__ __forceinline__ static float load(const float* p, float) { return *p; }
   __device__ __forceinline__ static void store(float* p, float v, float) { *p = v; }
+  __device__ __forceinline__ static float raw_load(const float* p) { return *p; }
+  __device__ __forceinline__ static void raw_store(float* p, float v) { *p = v; }
 };
 template <>
 struct Store<__nv_bfloat16> {
+  static constexpr int SH = 0;
   __device__ __forceinline__ static float load(const __nv_bfloat16* p, float) {
     return __bfloat162float(*p);
   }
   __device__ __forceinline__ static void store(__nv_bfloat16* p, float v, float) {
     *p = __float2bfloat16_rn(v);
   }
+  __device__ __forceinline__ static float raw_load(const __nv_bfloat16* p) {
+    return __bfloat162float(*p);
+  }
+  __device__ __forceinline__ static void raw_store(__nv_bfloat16* p, float v) {
+    *p = __float2bfloat16_rn(v);
+  }
 };
 template <>
 struct Store<__half> {
+  static constexpr int SH = FP16_SCALE_LOG2;
   __device__ __forceinline__ static float load(const __half* p, float scale) {
     return __half2float(*p) * (1.0f / scale);
   }
   __device__ __forceinline__ static void store(__half* p, float v, float scale) {
     *p = __float2half_rn(v * scale);
+  }
+  __device__ __forceinline__ static float raw_load(const __half* p) { return __half2float(*p); }
+  __device__ __forceinline__ static void raw_store(__half* p, float v) {
+    *p = __float2half_rn(v);
   }
 };
 
@@ -75,27 +93,37 @@ __device__ __forceinline__ float edot(int cx, int cy, int cz, float vx, float vy
 // The warp takes the plain BGK loop when none of its nodes is a PSM node,
 // the one-slot loop when none holds two particles, else the two-slot loop;
 // an unused slot has B = 0 and leaves f' bit-identical to the shorter loop.
-template <class L, bool FORCE, bool MACRO = true>
+//
+// SH > 0: f[] holds the deviations times S = 2^SH (FP16 storage's scale) and
+// is left scaled the same way.  Every quantity is then either the unscaled
+// one or exactly S times it (drho and j are summed scaled, the equilibrium
+// weights carry S); a power-of-two factor commutes with IEEE rounding, so
+// the results are bit for bit those of scaling on every load and store.
+template <class L, bool FORCE, bool MACRO = true, int SH = 0>
 __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const CollideParams& p,
                                                   const BoxParams& bp, long long n, uint8_t flag,
                                                   float4 r1, float4 r2) {
   constexpr int Q = L::Q;
-  float drho = -0.0f, jx = -0.0f, jy = -0.0f, jz = -0.0f;
+  constexpr float S = (float)(1 << SH), Si = 1.0f / (float)(1 << SH);
+  float dS = -0.0f, jx = -0.0f, jy = -0.0f, jz = -0.0f;  // scaled by S
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    drho += f[q];
+    dS += f[q];
     jx = sgn_add(jx, L::ex(q), f[q]);
     jy = sgn_add(jy, L::ey(q), f[q]);
     jz = sgn_add(jz, L::ez(q), f[q]);
   }
+  // the unscaling products are exact; __fmul_rn keeps them out of FMA
+  // contraction, which would round the neighbouring terms differently
+  const float drho = SH ? __fmul_rn(dS, Si) : dS;
   const float Fx = bp.F_f[0], Fy = bp.F_f[1], Fz = bp.F_f[2];
   if (FORCE) {
-    jx += 0.5f * Fx;
-    jy += 0.5f * Fy;
-    jz += 0.5f * Fz;
+    jx += (0.5f * S) * Fx;
+    jy += (0.5f * S) * Fy;
+    jz += (0.5f * S) * Fz;
   }
   const float rho = 1.0f + drho;
-  const float inv = __frcp_rn(rho);
+  const float inv = SH ? __fmul_rn(__frcp_rn(rho), Si) : __frcp_rn(rho);
   const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
   if (MACRO && p.store_macro) {
     p.rho_out[n] = 1.0 + (double)drho;
@@ -112,7 +140,7 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
   // BGK part of direction q: f + omega (feq - f) + F_q
 #define LBMPSM_BGK_Q(q)                                                              \
   const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);                            \
-  const float w = (float)L::w(q);                                                   \
+  const float w = (float)L::w(q) * S;                                               \
   const float eu = edot(cx, cy, cz, ux, uy, uz);                                    \
   const float geq = w * fmaf(rho * eu, fmaf(4.5f, eu, 3.0f), dr_u);                 \
   float bgk = fmaf(omega, geq - f[q], f[q]);                                        \
@@ -171,6 +199,11 @@ __device__ __forceinline__ void collide_node_lowp(float (&f)[L::Q], const Collid
   }
 #undef LBMPSM_BGK_Q
   if (psm) {
+    if (SH) {  // the node force needs j itself
+      jx = __fmul_rn(jx, Si);
+      jy = __fmul_rn(jy, Si);
+      jz = __fmul_rn(jz, Si);
+    }
     const float hx = 0.5f * omega * Fx, hy = 0.5f * omega * Fy, hz = 0.5f * omega * Fz;
     float* nf = static_cast<float*>(p.tab.nodeF) + 6 * n;
     nf[0] = -B1 * (fmaf(rho, s1x, -jx) + (FORCE ? hx : 0.0f));
@@ -199,17 +232,16 @@ __global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
   const Nbr nb = make_nbr(g, sx, sy, sz);
   T* __restrict__ F = static_cast<T*>(p.f);
   const long long Np = g.Np;
-  const float sc = p.scale16;
   float f[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
     const bool ok = nbr_ok(nb, -cx, -cy, -cz);
     if (!ODD) {
-      f[q] = ok ? Store<T>::load(F + q * Np + n, sc) : 0.0f;
+      f[q] = ok ? Store<T>::raw_load(F + q * Np + n) : 0.0f;
     } else {
       const int o = nbr_off(nb, -cx, -cy, -cz);
-      f[q] = ok ? Store<T>::load(F + L::opp(q) * Np + n + o, sc) : 0.0f;
+      f[q] = ok ? Store<T>::raw_load(F + L::opp(q) * Np + n + o) : 0.0f;
     }
   }
   const uint8_t flag = p.tab.flag[n];
@@ -218,14 +250,14 @@ __global__ void __launch_bounds__(128) collide_lowp_kernel(CollideParams p) {
     r1 = p.tab.rec32[2 * n];
     r2 = p.tab.rec32[2 * n + 1];
   }
-  collide_node_lowp<L, FORCE>(f, p, p.box[box_of_z(g, sz)], n, flag, r1, r2);
+  collide_node_lowp<L, FORCE, true, Store<T>::SH>(f, p, p.box[box_of_z(g, sz)], n, flag, r1, r2);
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int cx = L::ex(q), cy = L::ey(q), cz = L::ez(q);
     if (!ODD) {
-      Store<T>::store(F + L::opp(q) * Np + n, f[q], sc);
+      Store<T>::raw_store(F + L::opp(q) * Np + n, f[q]);
     } else {
-      if (nbr_ok(nb, cx, cy, cz)) Store<T>::store(F + q * Np + n + nbr_off(nb, cx, cy, cz), f[q], sc);
+      if (nbr_ok(nb, cx, cy, cz)) Store<T>::raw_store(F + q * Np + n + nbr_off(nb, cx, cy, cz), f[q]);
     }
   }
 }
@@ -503,7 +535,6 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
   const int xp = x < S0 - 1 ? x + 1 : 0;
   const bool vxm = x > 0 || g.per[0];
   const bool vxp = x < S0 - 1 || g.per[0];
-  const float sc = p.scale16;
   int cy = blockIdx.x % S1, cz = blockIdx.x / S1;
   int s = 0, ph = 0;
   for (int r = blockIdx.x; r < R; r += G) {
@@ -542,7 +573,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
         for (int q = 0; q < Q; ++q) {
           const int ex = L::ex(q);
           const int xs = ODD ? (ex == 0 ? x : (ex > 0 ? xm : xp)) : x;
-          f[q] = Store<T>::load(buf + q * P0 + xs, sc);
+          f[q] = Store<T>::raw_load(buf + q * P0 + xs);
         }
       } else {
 #pragma unroll
@@ -552,10 +583,10 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
           const bool okq =
               ((rows >> row_bit(-ey, -ez)) & 1u) && (ex == 0 || (ex > 0 ? vxm : vxp));
           const int xs = ODD ? (ex == 0 ? x : (ex > 0 ? xm : xp)) : x;
-          f[q] = okq ? Store<T>::load(buf + q * P0 + xs, sc) : 0.0f;
+          f[q] = okq ? Store<T>::raw_load(buf + q * P0 + xs) : 0.0f;
         }
       }
-      collide_node_lowp<L, FORCE>(f, p, p.box[box_of_z(g, cz)], n, flag, r1, r2);
+      collide_node_lowp<L, FORCE, true, Store<T>::SH>(f, p, p.box[box_of_z(g, cz)], n, flag, r1, r2);
     }
     // odd step: every input read before any output lands on a neighbour's
     // column (the even step reads and writes only the thread's own column)
@@ -563,13 +594,13 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
     if (active) {
       if (!ODD) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) Store<T>::store(buf + L::opp(q) * P0 + x, f[q], sc);
+        for (int q = 0; q < Q; ++q) Store<T>::raw_store(buf + L::opp(q) * P0 + x, f[q]);
       } else if (all_ok) {
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
           const int ex = L::ex(q);
           const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
-          Store<T>::store(buf + q * P0 + xt, f[q], sc);
+          Store<T>::raw_store(buf + q * P0 + xt, f[q]);
         }
       } else {
 #pragma unroll
@@ -577,7 +608,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
           const int ex = L::ex(q), ey = L::ey(q), ez = L::ez(q);
           const bool okq = ((rows >> row_bit(ey, ez)) & 1u) && (ex == 0 || (ex > 0 ? vxp : vxm));
           const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
-          if (okq) Store<T>::store(buf + q * P0 + xt, f[q], sc);
+          if (okq) Store<T>::raw_store(buf + q * P0 + xt, f[q]);
         }
       }
     }
@@ -773,7 +804,6 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 8) collide_multi_kernel(Mu
     const bool active = r < tr.k;
     const int xm = x > 0 ? x - 1 : S0 - 1;
     const int xp = x < S0 - 1 ? x + 1 : 0;
-    const float sc = p.scale16;
     const long long n = ((long long)tr.z * g.S[1] + tr.y0 + r) * P0 + x;
     uint8_t flag = 0;
     float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r1;
@@ -804,10 +834,10 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 8) collide_multi_kernel(Mu
       for (int q = 0; q < Q; ++q) {
         const int ex = L::ex(q);
         const int xs = ODD ? (ex == 0 ? x : (ex > 0 ? xm : xp)) : x;
-        f[q] = Store<T>::load(buf + q * tcp + xs, sc);
+        f[q] = Store<T>::raw_load(buf + q * tcp + xs);
       }
       // every member has a body force, or none has (the host checks)
-      collide_node_lowp<L, FORCE, false>(f, p, p.box[box_of_z(g, tr.z)], n, flag, r1, r2);
+      collide_node_lowp<L, FORCE, false, Store<T>::SH>(f, p, p.box[box_of_z(g, tr.z)], n, flag, r1, r2);
     }
     // odd step: every input read before any output lands on a neighbour's
     // column (the even step reads and writes only the thread's own column)
@@ -815,13 +845,13 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 8) collide_multi_kernel(Mu
     if (active) {
       if (!ODD) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) Store<T>::store(buf + L::opp(q) * tcp + x, f[q], sc);
+        for (int q = 0; q < Q; ++q) Store<T>::raw_store(buf + L::opp(q) * tcp + x, f[q]);
       } else {
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
           const int ex = L::ex(q);
           const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
-          Store<T>::store(buf + q * tcp + xt, f[q], sc);
+          Store<T>::raw_store(buf + q * tcp + xt, f[q]);
         }
       }
     }

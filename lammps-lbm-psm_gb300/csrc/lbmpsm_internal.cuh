@@ -218,7 +218,7 @@ struct CollideParams {
   const BoxParams* box;   // per-box BGK / Guo parameters (g.nbox entries)
   int has_force;          // any box with |F_lbm|^2 > 0
   double invCs2, invCs4;
-  float scale16;          // FP16 storage: stored value = deviation * scale16
+  float scale16;          // FP16 storage: stored value = deviation * scale16 (= 2^FP16_SCALE_LOG2)
   int* status;            // error word (STATUS_*)
   PipeConfig pipe;
   const void* fsrc;       // FP64 only: read the populations here and write f (null: in place)
@@ -234,6 +234,9 @@ struct CollideParams {
 // storage plane into a tile, so that small boxes fill the block's threads;
 // the FP64 kernel takes the members' (row, x-chunk) blocks in turn.  Members
 // must be 3-D and periodic on every axis.
+// FP16 storage keeps deviations scaled by 2^12; the collide kernels work on
+// the scaled values directly (a power-of-two scale commutes with rounding).
+constexpr int FP16_SCALE_LOG2 = 12;
 constexpr int MULTI_MAX = 16;
 struct MultiMember {
   CollideParams p;  // the member's own collide parameters

@@ -209,3 +209,34 @@ def test_fix_classes_drive_the_library(tmp_path):
     assert "flow_field.00000000.pvti" in files and "flow_field.00000000_rank0.vti" in files
     assert "flow_field.00000002_rank0.vti" in files and "flow_field.00000004_rank0.vti" in files
     assert "flow_field.00000003_rank0.vti" not in files
+
+
+@pytest.mark.parametrize("name", ["dense_periodic_3d", "c2_sphere_3d", "dense_periodic_2d"])
+def test_fp16_step_is_the_fp32_step_rounded(name):
+    """FP16 storage runs the FP32 collision on deviations kept scaled by 2^12
+    (the scale folded into the equilibrium weights): from one state, an FP16
+    step must give the FP32 step's populations rounded to FP16, bit for bit,
+    and the same forces.  Both lattices see the same images from the start,
+    so that their two-slot tables share the same history."""
+    case = cases.CASES[name]
+    tag, x, v, w, r = cases.initial_particles(case)
+    a = _lat(case, "fp16")
+    b = _lat(case, "fp32")
+    wq = b.populations().reshape(-1, b.q)[0].copy()  # at rest: f_q = w_q
+    for _ in range(6):
+        g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
+        a.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+        b.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+        x = cases.advance(case, x, v)
+    b.set_populations(a.populations())
+    g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
+    fa = a.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+    fb = b.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"])
+    for p, q in zip(fa, fb):
+        assert np.array_equal(p, q)
+    pa, pb = a.populations(), b.populations()
+    dev32 = (pb - wq).astype(np.float32)  # exact: the FP32 deviations
+    assert np.array_equal((pb - wq), dev32.astype(np.float64))
+    dev16 = (dev32 * np.float32(4096.0)).astype(np.float16).astype(np.float64) / 4096.0
+    assert np.count_nonzero(pa != wq) > 0  # a developed state, not rest
+    assert np.array_equal(pa, wq + dev16)
