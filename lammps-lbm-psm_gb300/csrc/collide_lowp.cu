@@ -1019,16 +1019,20 @@ static cudaError_t pipe_prepare(const Geom& g, int sm_count, PipeConfig* cfg) {
   return cudaSuccess;
 }
 
+// Blocks per multiprocessor the launch bounds ask for: three for two or three
+// stages (72 registers), two for four or five; with 16-bit storage a stage is
+// half as large and two or three stages run four blocks (56 registers, a few
+// spilled), which the measured 256^3 step favours by 7-10 us.
 template <class L, typename T>
 static cudaError_t prepare_lowp(const Geom& g, int sm_count, int stages, PipeConfig* cfg) {
   *cfg = PipeConfig{};
   if (g.S[0] > STAGED_MAX_ROW) return cudaSuccess;
   switch (stages) {
     case 0: return cudaSuccess;  // the direct kernel
-    case 2: return pipe_prepare<L, T, 2, 3>(g, sm_count, cfg);
+    case 2: return pipe_prepare<L, T, 2, sizeof(T) == 2 ? 4 : 3>(g, sm_count, cfg);
     case 4: return pipe_prepare<L, T, 4, 2>(g, sm_count, cfg);
     case 5: return pipe_prepare<L, T, 5, 2>(g, sm_count, cfg);
-    default: return pipe_prepare<L, T, 3, 3>(g, sm_count, cfg);
+    default: return pipe_prepare<L, T, 3, sizeof(T) == 2 ? 4 : 3>(g, sm_count, cfg);
   }
 }
 
@@ -1064,10 +1068,10 @@ template <class L, typename T>
 static cudaError_t launch_lowp(const CollideParams& p, int odd, cudaStream_t st) {
   if (p.pipe.grid > 0) {
     switch (p.pipe.stages) {
-      case 2: launch_pipe<L, T, 2, 3>(p, odd, st); break;
+      case 2: launch_pipe<L, T, 2, sizeof(T) == 2 ? 4 : 3>(p, odd, st); break;
       case 4: launch_pipe<L, T, 4, 2>(p, odd, st); break;
       case 5: launch_pipe<L, T, 5, 2>(p, odd, st); break;
-      default: launch_pipe<L, T, 3, 3>(p, odd, st); break;
+      default: launch_pipe<L, T, 3, sizeof(T) == 2 ? 4 : 3>(p, odd, st); break;
     }
     return cudaGetLastError();
   }
