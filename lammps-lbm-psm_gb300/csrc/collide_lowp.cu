@@ -366,9 +366,6 @@ __device__ __forceinline__ void next_row(int& sy, int& sz, int dy, int dz, int S
 __device__ __forceinline__ void mbar_arrive(unsigned bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
-__device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
-}
 // barrier over nthreads threads that also ANDs a predicate across them
 __device__ __forceinline__ bool named_bar_and(int id, int nthreads, bool v) {
   int r;
@@ -476,9 +473,13 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
         ok = __all_sync(0xffffffffu, mbar_wait_abortable(smem_addr(&done[ss]), sph, &s_abort));
         if (!ok) break;
         long long base = 0;
-        const bool ex = mine && (ODD ? row_of(g, sy, sz, ey, ez, base)
+        // back where it was loaded from (the odd step's outputs were written
+        // into the rows their locations came from)
+        const bool ex = mine && (ODD ? row_of(g, sy, sz, -ey, -ez, base)
                                      : (base = ((long long)sz * S1 + sy) * P0, true));
-        if (ex) bulk_store(F + lane * Np + base, smem0 + ss * stage_bytes + lane * row_bytes, row_bytes);
+        if (ex)
+          bulk_store(F + (ODD ? qo : lane) * Np + base, smem0 + ss * stage_bytes + lane * row_bytes,
+                     row_bytes);
         bulk_commit();
         next_row(sy, sz, gdy, gdz, S1);
         ++stored;
@@ -588,9 +589,11 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
       }
       collide_node_lowp<L, FORCE, true, Store<T>::SH>(f, p, p.box[box_of_z(g, cz)], n, flag, r1, r2);
     }
-    // odd step: every input read before any output lands on a neighbour's
-    // column (the even step reads and writes only the thread's own column)
-    if (ODD) named_bar_sync(1, ncons);
+    // Each thread writes only the shared-memory slots it read: the even step
+    // its own column; the odd step puts outgoing f_q at location (x + e_q, q),
+    // which the stage holds in row opp(q) (loaded from slot q of row y + e_q)
+    // at x + ex_q -- the slot this thread read as its incoming f_opp(q).  So
+    // no consumer barrier separates the reads from the writes.
     if (active) {
       if (!ODD) {
 #pragma unroll
@@ -600,7 +603,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
         for (int q = 0; q < Q; ++q) {
           const int ex = L::ex(q);
           const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
-          Store<T>::raw_store(buf + q * P0 + xt, f[q]);
+          Store<T>::raw_store(buf + L::opp(q) * P0 + xt, f[q]);
         }
       } else {
 #pragma unroll
@@ -608,7 +611,7 @@ __global__ void __launch_bounds__(STAGED_MAX_ROW + 32, MINB) collide_pipe_kernel
           const int ex = L::ex(q), ey = L::ey(q), ez = L::ez(q);
           const bool okq = ((rows >> row_bit(ey, ez)) & 1u) && (ex == 0 || (ex > 0 ? vxp : vxm));
           const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
-          if (okq) Store<T>::raw_store(buf + q * P0 + xt, f[q]);
+          if (okq) Store<T>::raw_store(buf + L::opp(q) * P0 + xt, f[q]);
         }
       }
     }
@@ -737,8 +740,8 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 8) collide_multi_kernel(Mu
           const unsigned row_bytes = (unsigned)(g.P0 * (int)sizeof(T));
           for (int r = 0; r < tr.k; ++r) {
             long long base = ((long long)tr.z * g.S[1] + tr.y0 + r) * g.P0;
-            if (ODD) row_of(g, tr.y0 + r, tr.z, ey, ez, base);
-            bulk_store(F + lane * g.Np + base,
+            if (ODD) row_of(g, tr.y0 + r, tr.z, -ey, -ez, base);  // where it was loaded from
+            bulk_store(F + (ODD ? qo : lane) * g.Np + base,
                        smem0 + ss * stage_bytes + (unsigned)((lane * tcp + r * g.P0) * (int)sizeof(T)),
                        row_bytes);
           }
@@ -839,9 +842,7 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 8) collide_multi_kernel(Mu
       // every member has a body force, or none has (the host checks)
       collide_node_lowp<L, FORCE, false, Store<T>::SH>(f, p, p.box[box_of_z(g, tr.z)], n, flag, r1, r2);
     }
-    // odd step: every input read before any output lands on a neighbour's
-    // column (the even step reads and writes only the thread's own column)
-    if (ODD) named_bar_sync(1, ncons);
+    // each thread writes only the slots it read (collide_pipe_kernel)
     if (active) {
       if (!ODD) {
 #pragma unroll
@@ -851,7 +852,7 @@ __global__ void __launch_bounds__(MULTI_MAX_ROW + 32, 8) collide_multi_kernel(Mu
         for (int q = 0; q < Q; ++q) {
           const int ex = L::ex(q);
           const int xt = ex == 0 ? x : (ex > 0 ? xp : xm);
-          Store<T>::raw_store(buf + q * tcp + xt, f[q]);
+          Store<T>::raw_store(buf + L::opp(q) * tcp + xt, f[q]);
         }
       }
     }
