@@ -211,10 +211,12 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
+def profile_traffic(storage="fp32"):
     """Per-launch DRAM traffic of the collide kernel at the bench size, from
-    the committed ncu summary (profiles/collide_f32_d3q19_256.md), else None."""
-    path = os.path.join(ROOT, "profiles", "collide_f32_d3q19_256.md")
+    the committed ncu summary of that storage
+    (profiles/collide_{f32,f16,bf16}_d3q19_256.md), else None."""
+    tag = {"fp32": "f32", "fp16": "f16", "bf16": "bf16"}[storage]
+    path = os.path.join(ROOT, "profiles", f"collide_{tag}_d3q19_256.md")
     try:
         for ln in open(path):
             if ln.startswith("traffic_bytes_per_launch:"):
@@ -363,7 +365,7 @@ def run_ours(args, rank=0, world=1):
     mlups = whole_job_mlups(nodes, K, world, t_val)
     peak, peak_kind = measured_peak_gbs()
     achieved = BYTES_PER_NODE[args.storage] * nodes / t_kernel / 1e9
-    traffic = profile_traffic()
+    traffic = profile_traffic(args.storage)
     # map: prep, scan, fill, sort, classify, shell, apply; collide; reduce; bc
     launches_per_step = 10
     out = {
@@ -395,7 +397,7 @@ def run_ours(args, rank=0, world=1):
                 "d2h_bytes_per_step": int(n * 12 * 8 + 4)},  # F/T/S + the status word
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": f"collide_pipe_kernel<D3Q19,{'float' if args.storage == 'fp32' else '__half'}> "
+                     "kernel": f"collide_pipe_kernel<D3Q19,{ {'fp32': 'float', 'fp16': '__half', 'bf16': '__nv_bfloat16'}[args.storage]}> "
                                "(warp-specialised row pipeline, A-A even/odd)",
                      "algorithmic_bytes_per_node": BYTES_PER_NODE[args.storage],
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
