@@ -415,62 +415,107 @@ static __device__ __forceinline__ float sub_offset(int k) {
   return -0.45f + 0.1f * small_int_to_float(k);  // within 1.7u of the reference's delta_k
 }
 
-// Phase 1 of the map, one block per image: every node of the image box is
-// classified by the early-out radii of calcSolidFraction; inside / outside
-// nodes get their code here, and so do shell nodes whose sub-cells all lie
-// on one side of the surface; the other shell nodes (whose sub-cells must be
-// counted) are queued in shared memory and appended to a global list with
-// one atomic per round of the block.
-constexpr int SFC_ROUND = 2048;
+// Phase 1 of the map, one block per image.  The box's codes are first set
+// to 0 with coalesced stores; then only the nodes of each x-row that may
+// lie within rP (an FP32 bound widened by 0.01 node: a superset of the
+// nodes classify_node does not put beyond rP for certain) are classified by
+// the early-out radii of calcSolidFraction.  Inside nodes get their code
+// here, and so do shell nodes whose sub-cells all lie on one side of the
+// surface; the other shell nodes (whose sub-cells must be counted) are
+// queued per warp in shared memory and appended to a global list with one
+// atomic per flush.  Each warp takes 32 rows at a time, one per lane, and
+// walks the nodes of their segments 32 at a time (consecutive lanes on
+// consecutive nodes of a row).
+constexpr int SFC_QW = 256;  // per-warp queue of shell nodes
 __global__ void __launch_bounds__(SFC_THREADS) sf_classify_kernel(MapParams p) {
   const Img& im = p.img[blockIdx.x];
   if (!im.valid) return;
   if (p.pair_total[0] > (unsigned long long)p.list_cap ||
       p.pair_total[1] > (unsigned long long)p.sf_cap)
     return;
-  __shared__ int q_li[SFC_ROUND], q_xy[SFC_ROUND], q_z[SFC_ROUND];
-  __shared__ int qn;
-  __shared__ unsigned long long qbase;
+  constexpr int NW = SFC_THREADS / 32;
+  __shared__ int4 q[NW][SFC_QW];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const Geom& g = p.g;
-  const int wx = im.box[0], wy = im.box[1];
-  const int vol = wx * wy * im.box[2];
+  const int wx = im.box[0], wy = im.box[1], wz = im.box[2];
+  const int vol = wx * wy * wz;
   unsigned short* code = p.sfcode + im.sf_off;
-  const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
-  for (int r0 = 0; r0 < vol; r0 += SFC_ROUND) {
-    if (threadIdx.x == 0) qn = 0;
-    __syncthreads();
-    const int r1 = min(vol, r0 + SFC_ROUND);
-    for (int li = r0 + threadIdx.x; li < r1; li += SFC_THREADS) {
-      const int q1 = (int)fast_div((unsigned)li, fx);
-      const int q2 = (int)fast_div((unsigned)q1, fy);
-      const int hx = im.lo[0] + li - q1 * wx + g.off[0];
-      const int hy = im.lo[1] + q1 - q2 * wy + g.off[1];
-      const int hz = im.lo[2] - im.zoff + q2 + g.off[2];  // z in the box's own frame
-      float dxf, dyf, dzf;
-      int c = classify_node(hx, hy, hz, im, dxf, dyf, dzf);
-      if (c < 0) c = corner_count(g.dim, dxf, dyf, dzf, im.rSqf);
-      if (c >= 0) {
-        code[li] = (unsigned short)c;
-      } else {
-        const int k = atomicAdd(&qn, 1);
-        q_li[k] = li;
-        q_xy[k] = hx | (hy << 16);
-        q_z[k] = hz;
-      }
-    }
-    __syncthreads();
-    const int nq = qn;
-    if (threadIdx.x == 0 && nq) qbase = atomicAdd(&p.pair_total[2], (unsigned long long)nq);
-    __syncthreads();
-    for (int k = threadIdx.x; k < nq; k += SFC_THREADS) {
-      const unsigned long long pos = qbase + k;
+  for (int li = threadIdx.x; li < vol; li += SFC_THREADS) code[li] = 0;
+  __syncthreads();  // the zeros land before any code of this block
+  // reference-frame coordinates of the box's first node
+  const int h0 = im.lo[0] + g.off[0], h1 = im.lo[1] + g.off[1];
+  const int h2 = im.lo[2] - im.zoff + g.off[2];  // z in the box's own frame
+  const float rem0 = im.rP2f * 1.0001f + 0.01f;
+  const FastDiv fy = make_fastdiv((unsigned)wy);
+  int qn = 0;  // entries in this warp's queue (warp-uniform)
+  auto flush = [&]() {
+    unsigned long long qb = 0;
+    if (lane == 0) qb = atomicAdd(&p.pair_total[2], (unsigned long long)qn);
+    qb = __shfl_sync(0xffffffffu, qb, 0);
+    for (int k = lane; k < qn; k += 32) {
+      const unsigned long long pos = qb + k;
       if (pos < (unsigned long long)p.shell_cap)
-        p.shell[pos] = make_int4((int)blockIdx.x, q_li[k], q_xy[k], q_z[k]);
+        p.shell[pos] = q[warp][k];
       else
         atomicOr(p.status, STATUS_LIST_OVERFLOW);
     }
-    __syncthreads();
+    __syncwarp();
+    qn = 0;
+  };
+  const int R = wy * wz;
+  for (int r0 = warp * 32; r0 < R; r0 += SFC_THREADS) {
+    const int r = r0 + lane;
+    int xa = 0, len = 0, by = 0, bz = 0;
+    if (r < R) {
+      bz = (int)fast_div((unsigned)r, fy);
+      by = r - bz * wy;
+      const float dy = small_int_to_float(h1 + by - im.xi[1]) - im.xf[1];
+      const float dz = small_int_to_float(h2 + bz - im.xi[2]) - im.xf[2];
+      const float rem = rem0 - dy * dy - dz * dz;
+      if (rem >= 0.0f) {
+        const float h = sqrtf(rem) + 0.01f;
+        xa = max(0, im.xi[0] + (int)ceilf(im.xf[0] - h) - h0);
+        const int xb = min(wx, im.xi[0] + (int)floorf(im.xf[0] + h) + 1 - h0);
+        len = max(xb - xa, 0);
+      }
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int excl = incl - len;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (int base = 0; base < total; base += 32) {
+      const int t = base + lane;
+      // the row holding node t: the last lane whose offset is <= t
+      int l = 0;
+#pragma unroll
+      for (int st = 16; st >= 1; st >>= 1)
+        if (__shfl_sync(0xffffffffu, excl, l + st) <= t) l += st;
+      const int ax = __shfl_sync(0xffffffffu, xa, l) + t - __shfl_sync(0xffffffffu, excl, l);
+      const int ay = __shfl_sync(0xffffffffu, by, l), az = __shfl_sync(0xffffffffu, bz, l);
+      const int hx = h0 + ax, hy = h1 + ay, hz = h2 + az;
+      const int li = (az * wy + ay) * wx + ax;
+      int c = 0;
+      if (t < total) {
+        float dxf, dyf, dzf;
+        c = classify_node(hx, hy, hz, im, dxf, dyf, dzf);
+        if (c < 0) c = corner_count(g.dim, dxf, dyf, dzf, im.rSqf);
+        if (c > 0) code[li] = (unsigned short)c;
+      }
+      const unsigned sm = __ballot_sync(0xffffffffu, c < 0);
+      if (sm) {
+        if (qn + 32 > SFC_QW) flush();
+        if (c < 0) q[warp][qn + __popc(sm & ((1u << lane) - 1u))] = make_int4((int)blockIdx.x, li,
+                                                                          hx | (hy << 16), hz);
+        qn += __popc(sm);
+        __syncwarp();
+      }
+    }
   }
+  if (qn) flush();
 }
 
 // Exact double of a small non-negative integer without the conversion unit.
@@ -1218,13 +1263,17 @@ static __device__ __forceinline__ void two_sum(float a, float b, float& s, float
   e = (a - (s - bb)) + (b - bb);
 }
 
-// FP32 node forces (FP32 / FP16 storage): per-node terms in FP32 (the node
-// forces carry FP32 precision), accumulated per particle in double-float
+// FP32 node forces (FP32 / FP16 / BF16 storage): per-node terms in FP32 (the
+// node forces carry FP32 precision), accumulated per particle in double-float
 // (hi + lo pairs combined with TwoSum, ~48-bit significand) on the FP32 pipe,
 // then the per-warp results summed in FP64.  (FP64 arithmetic runs at 1/64 of
-// the FP32 rate on this GPU.)  Latency-bound: 64 registers, 128-thread blocks
-// (8 per multiprocessor: 2281 images of the 256^3 suspension fill the GPU in
-// finer waves than 256-thread blocks) and two nodes' loads in flight per thread.
+// the FP32 rate on this GPU.)  Issue- and latency-bound: 64 registers,
+// 128-thread blocks (8 per multiprocessor: 2281 images of the 256^3
+// suspension fill the GPU in finer waves than 256-thread blocks), two nodes'
+// loads in flight per thread, and only the nodes of each row that may lie
+// within rP visited (a sphere holds about half of its box), without the
+// divergence of testing every box node.  The order of the sums is fixed by
+// the image's box alone, so the results are reproducible bit for bit.
 constexpr int RED_U = 2;
 __global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams p) {
   const int ip = blockIdx.x;
@@ -1235,78 +1284,121 @@ __global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams
   float hi[12], lo[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) hi[k] = lo[k] = 0.0f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (wx > 0 && wy > 0 && wz > 0) {
     const int xi[3] = {bx.xi[0], bx.xi[1], bx.xi[2]};  // xl = xi + xf exactly
     const float xf[3] = {bx.xf[0], bx.xf[1], bx.xf[2]};
-    const int total = wx * wy * wz;
     const float* nodeF = static_cast<const float*>(p.tab.nodeF);
-    // x fastest: consecutive threads read consecutive nodes
-    const FastDiv fx = make_fastdiv((unsigned)wx), fy = make_fastdiv((unsigned)wy);
-    // RED_U nodes per iteration: their ids and forces are loaded before any
-    // is summed (more loads in flight per thread); each thread still sums
-    // its nodes t, t + RED_THREADS, ... in that order
-    for (int t0 = threadIdx.x; t0 < total; t0 += RED_U * RED_THREADS) {
-      int2 id[RED_U];
-      float2 f01[RED_U], f23[RED_U], f45[RED_U];
-      float dx[RED_U], dy[RED_U], dz[RED_U];
-      bool ok[RED_U];
-#pragma unroll
-      for (int u = 0; u < RED_U; ++u) {
-        const int t = t0 + u * RED_THREADS;
-        const int q1 = (int)fast_div((unsigned)t, fx);
-        const int q2 = (int)fast_div((unsigned)q1, fy);
-        const int i = bx.qlo[0] + t - q1 * wx;
-        const int j = bx.qlo[1] + q1 - q2 * wy;
-        const int k = bx.qlo[2] + q2;
-        ok[u] = t < total && !(bx.solo && beyond_rP(bx, i, j, k));
-        id[u] = make_int2(0, 0);
-        f01[u] = f23[u] = f45[u] = make_float2(0.f, 0.f);
-        dx[u] = small_int_to_float(i - xi[0]) - xf[0];
-        dy[u] = small_int_to_float(j - xi[1]) - xf[1];
-        dz[u] = small_int_to_float(k - xi[2]) - xf[2];
-        if (ok[u]) {
-          const long long n = node_index(g, i - g.off[0], j - g.off[1], k - g.off[2] + bx.zoff);
-          // both slots' forces are loaded with the ids (no second dependent load)
-          id[u] = p.tab.ids[n];
-          const float2* nf2 = reinterpret_cast<const float2*>(nodeF + 6 * n);
-          f01[u] = nf2[0];
-          f23[u] = nf2[1];
-          f45[u] = nf2[2];
+    const int R = wy * wz;  // x-rows of the box
+    const FastDiv fy = make_fastdiv((unsigned)wy);
+    // A solo image's tag can only sit on nodes within rP (eps > 0 from this
+    // image), so each row is cut to the x-range that may lie within rP: an
+    // FP32 bound widened by 0.01 node, a superset (extra nodes fail the tag
+    // test).  Each warp takes 32 rows at a time, one per lane, and walks the
+    // nodes of their segments 32 at a time (x fastest, consecutive lanes on
+    // consecutive nodes); a lane finds its node's row by a binary search of
+    // the segments' offsets across the warp.
+    const float rem0 = bx.rP2f * 1.0001f + 0.01f;
+    for (int r0 = warp * 32; r0 < R; r0 += RED_THREADS) {
+      const int r = r0 + lane;
+      int xa = bx.qlo[0], len = 0, j = 0, k = 0;
+      if (r < R) {
+        const int q = (int)fast_div((unsigned)r, fy);
+        j = bx.qlo[1] + r - q * wy;
+        k = bx.qlo[2] + q;
+        int xb = bx.qhi[0];
+        if (bx.solo) {
+          const float dy = small_int_to_float(j - xi[1]) - xf[1];
+          const float dz = small_int_to_float(k - xi[2]) - xf[2];
+          const float rem = rem0 - dy * dy - dz * dz;
+          if (rem < 0.0f) {
+            xb = xa;
+          } else {
+            const float h = sqrtf(rem) + 0.01f;
+            xa = max(xa, xi[0] + (int)ceilf(xf[0] - h));
+            xb = min(xb, xi[0] + (int)floorf(xf[0] + h) + 1);
+          }
         }
+        len = max(xb - xa, 0);
       }
+      int incl = len;
 #pragma unroll
-      for (int u = 0; u < RED_U; ++u) {
-        if (!ok[u]) continue;
-        float F0, F1, F2;
-        if (tag == id[u].x) {
-          F0 = f01[u].x;
-          F1 = f01[u].y;
-          F2 = f23[u].x;
-        } else if (tag == id[u].y) {
-          F0 = f23[u].y;
-          F1 = f45[u].x;
-          F2 = f45[u].y;
-        } else {
-          continue;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int excl = incl - len;
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      // RED_U nodes per lane and round, loaded before any is summed
+      for (int base = 0; base < total; base += RED_U * 32) {
+        int2 id[RED_U];
+        float2 f01[RED_U], f23[RED_U], f45[RED_U];
+        float dx[RED_U], dy[RED_U], dz[RED_U];
+        bool ok[RED_U];
+#pragma unroll
+        for (int u = 0; u < RED_U; ++u) {
+          const int t = base + u * 32 + lane;
+          // the row holding node t: the last lane whose offset is <= t (a
+          // row of length 0 shares its offset with the next row)
+          int l = 0;
+#pragma unroll
+          for (int st = 16; st >= 1; st >>= 1)
+            if (__shfl_sync(0xffffffffu, excl, l + st) <= t) l += st;
+          const int ra = __shfl_sync(0xffffffffu, xa, l);
+          const int re = __shfl_sync(0xffffffffu, excl, l);
+          const int jj = __shfl_sync(0xffffffffu, j, l);
+          const int kk = __shfl_sync(0xffffffffu, k, l);
+          const int i = ra + t - re;
+          ok[u] = t < total;
+          id[u] = make_int2(0, 0);
+          f01[u] = f23[u] = f45[u] = make_float2(0.f, 0.f);
+          dx[u] = small_int_to_float(i - xi[0]) - xf[0];
+          dy[u] = small_int_to_float(jj - xi[1]) - xf[1];
+          dz[u] = small_int_to_float(kk - xi[2]) - xf[2];
+          if (ok[u]) {
+            const long long n = node_index(g, i - g.off[0], jj - g.off[1], kk - g.off[2] + bx.zoff);
+            // both slots' forces are loaded with the ids (no second dependent load)
+            id[u] = p.tab.ids[n];
+            const float2* nf2 = reinterpret_cast<const float2*>(nodeF + 6 * n);
+            f01[u] = nf2[0];
+            f23[u] = nf2[1];
+            f45[u] = nf2[2];
+          }
         }
-        const float term[12] = {F0,
-                                F1,
-                                F2,
-                                dy[u] * F2 - dz[u] * F1,
-                                dz[u] * F0 - dx[u] * F2,
-                                dx[u] * F1 - dy[u] * F0,
-                                dx[u] * F0,
-                                dy[u] * F1,
-                                dz[u] * F2,
-                                0.5f * (dy[u] * F0 + dx[u] * F1),
-                                0.5f * (dz[u] * F0 + dx[u] * F2),
-                                0.5f * (dz[u] * F1 + dy[u] * F2)};
 #pragma unroll
-        for (int q = 0; q < 12; ++q) {
-          float sv, e;
-          two_sum(hi[q], term[q], sv, e);
-          hi[q] = sv;
-          lo[q] += e;
+        for (int u = 0; u < RED_U; ++u) {
+          if (!ok[u]) continue;
+          float F0, F1, F2;
+          if (tag == id[u].x) {
+            F0 = f01[u].x;
+            F1 = f01[u].y;
+            F2 = f23[u].x;
+          } else if (tag == id[u].y) {
+            F0 = f23[u].y;
+            F1 = f45[u].x;
+            F2 = f45[u].y;
+          } else {
+            continue;
+          }
+          const float term[12] = {F0,
+                                  F1,
+                                  F2,
+                                  dy[u] * F2 - dz[u] * F1,
+                                  dz[u] * F0 - dx[u] * F2,
+                                  dx[u] * F1 - dy[u] * F0,
+                                  dx[u] * F0,
+                                  dy[u] * F1,
+                                  dz[u] * F2,
+                                  0.5f * (dy[u] * F0 + dx[u] * F1),
+                                  0.5f * (dz[u] * F0 + dx[u] * F2),
+                                  0.5f * (dz[u] * F1 + dy[u] * F2)};
+#pragma unroll
+          for (int q = 0; q < 12; ++q) {
+            float sv, e;
+            two_sum(hi[q], term[q], sv, e);
+            hi[q] = sv;
+            lo[q] += e;
+          }
         }
       }
     }
@@ -1314,7 +1406,6 @@ __global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams
   // fixed-order double-float reduction within the warp: the first two levels
   // halve the terms each lane carries (12 -> 6 -> 3, partners keeping
   // complementary halves), the last three are a butterfly on three terms
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool up16 = (lane & 16) != 0, up8 = (lane & 8) != 0;
   float h6[6], l6[6], h3[3], l3[3];
 #pragma unroll
