@@ -1033,7 +1033,7 @@ static __device__ __forceinline__ float4 spin_velocity(const Img& im, int hi, in
 // and slot record loads are independent.  The slot ids are loaded with the
 // cell's count and offset, so that they add no round of dependent loads.
 template <int NPT>
-__global__ void __launch_bounds__(512 / NPT, 6) node_apply32_kernel(MapParams p) {
+__global__ void __launch_bounds__(512 / NPT, 8) node_apply32_kernel(MapParams p) {
   const int c = (blockIdx.z * p.C[1] + blockIdx.y) * p.C[0] + blockIdx.x;
   const Geom& g = p.g;
   const int sx = blockIdx.x * p.cb[0] + threadIdx.x;
