@@ -18,9 +18,12 @@ as the host DEM's motion would make it do.
 Prints one JSON line on rank 0.  `value` is measured with the images'
 positions resident in HBM (one set per step of the loops) and handed to
 lbmpsm_step_device each step, which the library replays as a CUDA graph;
-`e2e` runs the same steps through the host-pointer C-ABI call (images copied
-up from pinned memory and forces copied back every step, also one graph per
-step).  The lattice (1.27 GB in FP32) is ~10x larger than L2, so no L2 flush
+`e2e` runs the same steps through the host-pointer C-ABI call, also one graph
+per step: on GB300 the gather kernel reads the caller's image arrays and the
+reduction writes the forces into the caller's arrays over NVLink-C2C
+(pageable host memory through the host page tables, no staging copies);
+`e2e_staged` is the same call with LBMPSM_HOST_STAGING=1 (images copied into
+pinned memory and up, forces copied back).  The lattice (1.27 GB in FP32) is ~10x larger than L2, so no L2 flush
 is needed between steps.  `--impl reference` times the CPU oracle (the
 reference algorithm restated in C, FP64, all host cores) on the same
 workload.  `--workload ensemble` and `--workload adjoint` time the batched
@@ -335,6 +338,24 @@ def run_ours(args, rank=0, world=1):
         mov.host_step(lat, k)
     lat.synchronize()
     t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_direct = bool(lat.host_direct)
+
+    # the same through pinned staging copies (the path without C2C access)
+    os.environ["LBMPSM_HOST_STAGING"] = "1"
+    try:
+        stg = make(args.storage)
+    finally:
+        del os.environ["LBMPSM_HOST_STAGING"]
+    assert not stg.host_direct
+    for k in range(0, 1 + max(W, 3)):
+        mov.host_step(stg, k)
+    stg.synchronize()
+    t0 = time.perf_counter()
+    for k in range(1 + max(W, 3), 1 + max(W, 3) + K):
+        mov.host_step(stg, k)
+    stg.synchronize()
+    t_stg = max_over_ranks(time.perf_counter() - t0, world)
+    stg.close()
 
     # the collide-stream kernel alone: lattice-only steps (no images, so the
     # step launches only the collide kernel; the particle table stays in place)
@@ -394,7 +415,13 @@ def run_ours(args, rank=0, world=1):
         },
         "e2e": {"value": round(whole_job_mlups(nodes, K, world, t_e2e), 1), "unit": "MLUPS",
                 "h2d_bytes_per_step": int(n * (4 + 10 * 8)),
-                "d2h_bytes_per_step": int(n * 12 * 8 + 4)},  # F/T/S + the status word
+                "d2h_bytes_per_step": int(n * 12 * 8 + 4),  # F/T/S + the status word
+                "transfer": ("read and written by the step's kernels over NVLink-C2C (pageable "
+                             "host memory through the host page tables)" if e2e_direct else
+                             "pinned staging copies")},
+        "e2e_staged": {"value": round(whole_job_mlups(nodes, K, world, t_stg), 1), "unit": "MLUPS",
+                       "transfer": "images copied into pinned memory and up, forces copied back "
+                                   "(LBMPSM_HOST_STAGING=1)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": f"collide_pipe_kernel<D3Q19,{ {'fp32': 'float', 'fp16': '__half', 'bf16': '__nv_bfloat16'}[args.storage]}> "

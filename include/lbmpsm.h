@@ -213,6 +213,15 @@ int lbmpsm_synchronize(lbmpsm_handle* h);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their
  * own device work after *_device calls. */
 void* lbmpsm_stream(lbmpsm_handle* h);
+/* 1 when lbmpsm_step works on the caller's host arrays in place: the device
+ * reads pageable host memory through the host's page tables (NVLink-C2C on
+ * Grace), so the step's gather kernel reads the images and its reduction
+ * writes fh, th and stresslet with no staging copies; 0 when the images are
+ * staged through pinned memory and copied (devices without that access, or
+ * the environment variable LBMPSM_HOST_STAGING=1 at lbmpsm_create); -1 for
+ * a NULL handle.  Both give the same results bit for bit.  Single-box
+ * handles only: lbmpsm_step_batch always stages. */
+int lbmpsm_host_direct(const lbmpsm_handle* h);
 
 /* Run nsteps coupling steps with the particle images already on the device
  * (as last passed to lbmpsm_step or lbmpsm_step_device), fixed in place,

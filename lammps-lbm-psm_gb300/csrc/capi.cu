@@ -41,6 +41,12 @@ struct lbmpsm_handle {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_bc_fork = nullptr, ev_bc_join = nullptr;  // the BC beside the reduction
   float scale16 = (float)(1 << FP16_SCALE_LOG2);
+  // host-pointer steps without staging copies: the device reads and writes
+  // pageable host memory through the host's page tables (NVLink-C2C on
+  // Grace), so the gather kernel takes the caller's image arrays and the
+  // reduction writes the caller's outputs and status_host directly
+  bool host_direct = false;
+  int status_host = 0;
   // lattice
   void* f = nullptr;
   Table tab{};
@@ -592,6 +598,8 @@ int enqueue_post(lbmpsm_handle* h, int n, bool bc) {
     rp.fh2 = h->out2[0];
     rp.th2 = h->out2[1];
     rp.S2 = h->out2[2];
+    rp.status = h->d_status;
+    rp.status_out = h->host_direct ? &h->status_host : nullptr;
     CUDA_TRY(h, launch_reduce(rp, h->stream));
   }
   if (bc_aside) CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->ev_bc_join, 0));
@@ -895,6 +903,15 @@ int create_impl(int nbox, const lbmpsm_fix_params* ps, const lbmpsm_options* opt
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess)
     return bail(LBMPSM_ERR_CUDA);
   h->sm_count = std::max(sms, 1);
+  {
+    int pageable = 0, host_tables = 0;
+    const char* e = std::getenv("LBMPSM_HOST_STAGING");
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, o.device) == cudaSuccess &&
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                               o.device) == cudaSuccess)
+      h->host_direct = pageable == 1 && host_tables == 1 && !(e && e[0] == '1');
+    cudaGetLastError();
+  }
   if (o.storage != LBMPSM_STORAGE_FP64) {
     // launch shape of the collide kernel: LBMPSM_PIPE_STAGES if set (0 = direct
     // kernel, 2..5 stages), else the autotuner or the 3-stage default
@@ -1090,6 +1107,102 @@ int stage_images(lbmpsm_handle* h, int n, const int* box, const int* tag, const 
   return upload ? upload_images(h, n) : LBMPSM_OK;
 }
 
+// One step from image arrays the device can read (device memory, or host
+// memory when host_direct) into output arrays it can write: the gather
+// kernel copies the images into the handle's buffers, the reduction writes
+// the outputs beside the handle's own.  Asynchronous on the handle's stream.
+int device_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
+                const double* omega, const double* radius, double* fh, double* th,
+                double* stresslet) {
+  auto enqueue_all = [&]() -> int {
+    CUDA_TRY(h, launch_gather_images(n, tag, x, v, omega, radius, h->d_tag, h->d_xvw, h->stream));
+    h->out2[0] = n > 0 ? fh : nullptr;
+    h->out2[1] = n > 0 ? th : nullptr;
+    h->out2[2] = n > 0 ? stresslet : nullptr;
+    const int r = enqueue_step(h, n);
+    h->out2[0] = h->out2[1] = h->out2[2] = nullptr;
+    return r;
+  };
+  // Replayed as one CUDA graph per parity once the image count has held for
+  // two calls (as host steps are); each call writes its own pointers into the
+  // gather and reduce nodes of the executable graph, which affects only the
+  // launches that follow.  Steps that store the macroscopic fields, and steps
+  // without images, run eagerly.
+  h->dsame = n == h->dprev_n ? h->dsame + 1 : 0;
+  h->dprev_n = n;
+  if (n == 0 || h->macro_requested || (h->dgraph_n != n && h->dsame < 2)) return enqueue_all();
+  if (h->dgraph_n != n) drop_device_graphs(h);
+  const int par = (int)(h->t & 1);
+  if (!h->dexec[par]) {
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long t0 = h->t;
+    const int rc = enqueue_all();
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    h->t = t0;  // captured, not run
+    if (rc) {
+      if (ce == cudaSuccess && graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CUDA_TRY(h, ce);
+    // the nodes whose arguments change per call
+    size_t nn = 0;
+    cudaError_t e = cudaGraphGetNodes(graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (e == cudaSuccess) e = cudaGraphGetNodes(graph, nodes.data(), &nn);
+    cudaGraphNode_t gn = nullptr, rn = nullptr;
+    const void* fg = gather_images_fn();
+    const void* fr = reduce_fn(h->opt.storage == LBMPSM_STORAGE_FP64 ? 1 : 0);
+    for (size_t k = 0; e == cudaSuccess && k < nn; ++k) {
+      cudaGraphNodeType ty;
+      if (cudaGraphNodeGetType(nodes[k], &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp{};
+      if (cudaGraphKernelNodeGetParams(nodes[k], &kp) != cudaSuccess) continue;
+      if (kp.func == fg) gn = nodes[k];
+      if (kp.func == fr) rn = nodes[k];
+    }
+    cudaGraphExec_t ex = nullptr;
+    if (e == cudaSuccess && gn && rn) e = cudaGraphInstantiate(&ex, graph, 0);
+    if (e != cudaSuccess || !gn || !rn) {
+      cudaGetLastError();
+      cudaGraphDestroy(graph);
+      CUDA_TRY(h, e);
+      return fail(h, LBMPSM_ERR_CUDA, "device-step graph: the gather or reduce node was not found");
+    }
+    h->dgraph[par] = graph;
+    h->dexec[par] = ex;
+    h->dgather[par] = gn;
+    h->dreduce[par] = rn;
+    h->dgraph_n = n;
+  }
+  {
+    // this call's pointers into the gather and reduce nodes
+    cudaKernelNodeParams kp{};
+    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dgather[par], &kp));
+    int* dt = h->d_tag;
+    double* dxvw = h->d_xvw;
+    void* ga[] = {(void*)&n, (void*)&tag, (void*)&x, (void*)&v, (void*)&omega, (void*)&radius,
+                  (void*)&dt, (void*)&dxvw};
+    kp.kernelParams = ga;
+    kp.extra = nullptr;
+    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dgather[par], &kp));
+    cudaKernelNodeParams rk{};
+    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dreduce[par], &rk));
+    ReduceParams rp = *static_cast<const ReduceParams*>(rk.kernelParams[0]);
+    rp.fh2 = fh;
+    rp.th2 = th;
+    rp.S2 = stresslet;
+    void* ra[] = {(void*)&rp};
+    rk.kernelParams = ra;
+    rk.extra = nullptr;
+    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dreduce[par], &rk));
+  }
+  CUDA_TRY(h, cudaGraphLaunch(h->dexec[par], h->stream));
+  h->t += 1;
+  h->last_n = n;
+  return LBMPSM_OK;
+}
+
 // one coupling step with host arrays; box (may be null) gives each image's box
 //
 // The device work of a step with images -- upload of the staged images, map,
@@ -1108,6 +1221,23 @@ int step_impl(lbmpsm_handle* h, int n, const int* box, const int* tag, const dou
     return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
   int rc = maybe_tune(h);
   if (rc) return rc;
+  if (h->host_direct && !box && h->nbox == 1 && n > 0) {
+    // no staging: the device-step graph on the caller's host arrays
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    double rmax = 0.0;
+    for (int i = 0; i < n; ++i) rmax = std::max(rmax, radius[i]);
+    if (!finite_all(x, 3 * (size_t)n) || !std::isfinite(rmax))
+      return fail(h, LBMPSM_ERR_NUMERIC, "non-finite particle position or radius");
+    rc = ensure_particles(h, n, std::max(rmax, h->opt.max_radius));
+    if (rc) return rc;
+    if (h->step_boxes) drop_graphs(h);
+    h->step_boxes = false;
+    h->status_host = 0;
+    rc = device_step(h, n, tag, x, v, omega, radius, fh, th, stresslet);
+    if (rc) return rc;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return h->status_host ? read_status(h) : LBMPSM_OK;
+  }
   rc = stage_images(h, n, box, tag, x, v, omega, radius, /*upload=*/false);
   if (rc) return rc;
   const Stage sg = stage_of(h);
@@ -1202,95 +1332,7 @@ int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
   h->step_boxes = false;
   if (n > 0 && (!tag || !x || !v || !omega || !radius))
     return fail(h, LBMPSM_ERR_ARG, "NULL particle array");
-  // the images into the handle's buffers in one launch; the reduction writes
-  // the outputs into the caller's buffers beside the handle's own
-  auto enqueue_all = [&]() -> int {
-    CUDA_TRY(h, launch_gather_images(n, tag, x, v, omega, radius, h->d_tag, h->d_xvw, h->stream));
-    h->out2[0] = n > 0 ? fh : nullptr;
-    h->out2[1] = n > 0 ? th : nullptr;
-    h->out2[2] = n > 0 ? stresslet : nullptr;
-    const int r = enqueue_step(h, n);
-    h->out2[0] = h->out2[1] = h->out2[2] = nullptr;
-    return r;
-  };
-  // Replayed as one CUDA graph per parity once the image count has held for
-  // two calls (as host steps are); each call writes its own pointers into the
-  // gather and reduce nodes of the executable graph, which affects only the
-  // launches that follow.  Steps that store the macroscopic fields, and steps
-  // without images, run eagerly.
-  h->dsame = n == h->dprev_n ? h->dsame + 1 : 0;
-  h->dprev_n = n;
-  if (n == 0 || h->macro_requested || (h->dgraph_n != n && h->dsame < 2)) return enqueue_all();
-  if (h->dgraph_n != n) drop_device_graphs(h);
-  const int par = (int)(h->t & 1);
-  if (!h->dexec[par]) {
-    cudaGraph_t graph = nullptr;
-    CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    const long long t0 = h->t;
-    const int rc = enqueue_all();
-    const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
-    h->t = t0;  // captured, not run
-    if (rc) {
-      if (ce == cudaSuccess && graph) cudaGraphDestroy(graph);
-      return rc;
-    }
-    CUDA_TRY(h, ce);
-    // the nodes whose arguments change per call
-    size_t nn = 0;
-    cudaError_t e = cudaGraphGetNodes(graph, nullptr, &nn);
-    std::vector<cudaGraphNode_t> nodes(nn);
-    if (e == cudaSuccess) e = cudaGraphGetNodes(graph, nodes.data(), &nn);
-    cudaGraphNode_t gn = nullptr, rn = nullptr;
-    const void* fg = gather_images_fn();
-    const void* fr = reduce_fn(h->opt.storage == LBMPSM_STORAGE_FP64 ? 1 : 0);
-    for (size_t k = 0; e == cudaSuccess && k < nn; ++k) {
-      cudaGraphNodeType ty;
-      if (cudaGraphNodeGetType(nodes[k], &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
-      cudaKernelNodeParams kp{};
-      if (cudaGraphKernelNodeGetParams(nodes[k], &kp) != cudaSuccess) continue;
-      if (kp.func == fg) gn = nodes[k];
-      if (kp.func == fr) rn = nodes[k];
-    }
-    cudaGraphExec_t ex = nullptr;
-    if (e == cudaSuccess && gn && rn) e = cudaGraphInstantiate(&ex, graph, 0);
-    if (e != cudaSuccess || !gn || !rn) {
-      cudaGetLastError();
-      cudaGraphDestroy(graph);
-      CUDA_TRY(h, e);
-      return fail(h, LBMPSM_ERR_CUDA, "device-step graph: the gather or reduce node was not found");
-    }
-    h->dgraph[par] = graph;
-    h->dexec[par] = ex;
-    h->dgather[par] = gn;
-    h->dreduce[par] = rn;
-    h->dgraph_n = n;
-  }
-  {
-    // this call's pointers into the gather and reduce nodes
-    cudaKernelNodeParams kp{};
-    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dgather[par], &kp));
-    int* dt = h->d_tag;
-    double* dxvw = h->d_xvw;
-    void* ga[] = {(void*)&n, (void*)&tag, (void*)&x, (void*)&v, (void*)&omega, (void*)&radius,
-                  (void*)&dt, (void*)&dxvw};
-    kp.kernelParams = ga;
-    kp.extra = nullptr;
-    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dgather[par], &kp));
-    cudaKernelNodeParams rk{};
-    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dreduce[par], &rk));
-    ReduceParams rp = *static_cast<const ReduceParams*>(rk.kernelParams[0]);
-    rp.fh2 = fh;
-    rp.th2 = th;
-    rp.S2 = stresslet;
-    void* ra[] = {(void*)&rp};
-    rk.kernelParams = ra;
-    rk.extra = nullptr;
-    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dreduce[par], &rk));
-  }
-  CUDA_TRY(h, cudaGraphLaunch(h->dexec[par], h->stream));
-  h->t += 1;
-  h->last_n = n;
-  return LBMPSM_OK;
+  return device_step(h, n, tag, x, v, omega, radius, fh, th, stresslet);
 }
 
 int lbmpsm_apply_bc(lbmpsm_handle* h) {
@@ -1415,6 +1457,8 @@ int lbmpsm_synchronize(lbmpsm_handle* h) {
 }
 
 void* lbmpsm_stream(lbmpsm_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int lbmpsm_host_direct(const lbmpsm_handle* h) { return h ? (h->host_direct ? 1 : 0) : -1; }
 
 int lbmpsm_run_fixed(lbmpsm_handle* h, int nsteps) {
   if (!h || nsteps < 0) return LBMPSM_ERR_ARG;

@@ -360,9 +360,11 @@ struct ReduceParams {
   double* fh;
   double* th;
   double* S;
-  double* fh2;        // optional second copies of the outputs (the caller's device
-  double* th2;        // buffers of lbmpsm_step_device), written with the first
-  double* S2;
+  double* fh2;        // optional second copies of the outputs (the caller's
+  double* th2;        // buffers of lbmpsm_step_device or, read over NVLink-C2C,
+  double* S2;         // of lbmpsm_step), written with the first
+  const int* status;  // the step's status word (device)
+  int* status_out;    // optional host-visible copy of it, written by block 0 last
 };
 
 // status bits

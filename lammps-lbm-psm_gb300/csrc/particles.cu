@@ -1172,6 +1172,13 @@ static __device__ __forceinline__ bool beyond_rP(const Img& im, int i, int j, in
   return d32 > im.rP2f + m;
 }
 
+// The step's status word into host memory for the host-pointer step (every
+// kernel that sets a bit ran before the reduction in stream order).
+static __device__ __forceinline__ void copy_status(const ReduceParams& p) {
+  if (p.status_out && blockIdx.x == 0 && threadIdx.x == 0)
+    *p.status_out = *static_cast<const volatile int*>(p.status);
+}
+
 static __device__ __forceinline__ void block_reduce_store(double (&acc)[12], const ReduceParams& p,
                                                           int ip) {
   // fixed-order reduction: butterfly within warps, then warps in index order
@@ -1253,6 +1260,7 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_f64_kernel(ReduceParams p)
     }
   }
   block_reduce_store(acc, p, ip);
+  copy_status(p);
 }
 
 // Error-free transformation: a + b = s + e exactly (Knuth's TwoSum; no
@@ -1477,6 +1485,7 @@ __global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams
       if (p.S2) p.S2[6 * ip + (q - 6)] = v;
     }
   }
+  copy_status(p);
 }
 
 cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st) {

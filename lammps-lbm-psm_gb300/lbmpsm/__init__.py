@@ -38,6 +38,7 @@ SYMBOLS = (
     "lbmpsm_step", "lbmpsm_step_device", "lbmpsm_apply_bc", "lbmpsm_request_macro",
     "lbmpsm_export_fields", "lbmpsm_get_populations", "lbmpsm_set_populations",
     "lbmpsm_get_particle_table", "lbmpsm_check", "lbmpsm_synchronize", "lbmpsm_stream",
+    "lbmpsm_host_direct",
     "lbmpsm_run_fixed", "lbmpsm_read_forces", "lbmpsm_export_fields_static",
     "lbmpsm_create_batch", "lbmpsm_step_batch", "lbmpsm_select_box",
     "lbmpsm_adjoint_drag", "lbmpsm_tangent_drag",
@@ -116,6 +117,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.lbmpsm_synchronize.argtypes = [H]
     lib.lbmpsm_stream.argtypes = [H]
     lib.lbmpsm_stream.restype = C.c_void_p
+    lib.lbmpsm_host_direct.argtypes = [H]
     lib.lbmpsm_run_fixed.argtypes = [H, C.c_int]
     lib.lbmpsm_read_forces.argtypes = [H, C.c_int, _D, _D, _D]
     lib.lbmpsm_export_fields_static.argtypes = [H, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -300,6 +302,12 @@ class Lattice:
     @property
     def stream(self) -> int:
         return int(self.lib.lbmpsm_stream(self.h) or 0)
+
+    @property
+    def host_direct(self) -> bool:
+        """Host-pointer steps read and write the caller's arrays in place
+        (no staging copies); see lbmpsm_host_direct."""
+        return self.lib.lbmpsm_host_direct(self.h) == 1
 
     # -- fields and state
     def request_macro(self):

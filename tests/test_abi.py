@@ -64,6 +64,7 @@ def test_group_and_sensitivity_argument_checks_without_touching_the_gpu():
     assert lib.lbmpsm_group_create(arr, 2, C.byref(g)) == lbmpsm.ERR_ARG
     assert lib.lbmpsm_group_run_fixed(None, 1) == lbmpsm.ERR_ARG
     assert lib.lbmpsm_group_collide_launches(None) == -1
+    assert lib.lbmpsm_host_direct(None) == -1
     assert lib.lbmpsm_group_tune_ms(None, None) == lbmpsm.ERR_ARG
     assert lib.lbmpsm_adjoint_drag(None, 0, None, None, None, None, None, 10, 1, 10, None, 5,
                                    1e-4, None, None, None, None, None) == lbmpsm.ERR_ARG

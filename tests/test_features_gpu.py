@@ -240,3 +240,34 @@ def test_fp16_step_is_the_fp32_step_rounded(name):
     dev16 = (dev32 * np.float32(4096.0)).astype(np.float16).astype(np.float64) / 4096.0
     assert np.count_nonzero(pa != wq) > 0  # a developed state, not rest
     assert np.array_equal(pa, wq + dev16)
+
+
+@pytest.mark.parametrize("storage", ["fp64", "fp32"])
+def test_host_steps_in_place_equal_staged_steps(storage, monkeypatch):
+    """Host-pointer steps on a device that reads pageable host memory take
+    the caller's arrays in place (gather kernel and reduction over
+    NVLink-C2C); LBMPSM_HOST_STAGING=1 stages them through pinned copies.
+    Both give the same forces and populations bit for bit, through the
+    eager first steps and the replayed graphs, with the image count
+    changing on the way; a non-finite position is still rejected."""
+    case = cases.CASES["shear_3d"]
+    tag, x, v, w, r = cases.initial_particles(case)
+    a = _lat(case, storage)
+    monkeypatch.setenv("LBMPSM_HOST_STAGING", "1")
+    b = _lat(case, storage)
+    monkeypatch.delenv("LBMPSM_HOST_STAGING")
+    assert not b.host_direct
+    for _ in range(9):
+        g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
+        fa = a.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"]); a.apply_bc()
+        fb = b.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"]); b.apply_bc()
+        for p, q in zip(fa, fb):
+            assert np.array_equal(p, q)
+        x = cases.advance(case, x, v)
+    assert np.array_equal(a.populations(), b.populations())
+    # non-finite input: rejected on the host before any device work
+    g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
+    bad = np.array(g["x"], dtype=np.float64)
+    bad[0, 0] = np.nan
+    with pytest.raises(lbmpsm.LbmPsmError):
+        a.step(g["tag"], bad, g["v"], g["omega"], g["radius"])
