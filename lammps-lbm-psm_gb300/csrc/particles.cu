@@ -70,7 +70,12 @@ static __device__ __forceinline__ void reduce_box_of(const Geom& g, const double
 // src/LBM_PSM_exchangeParticleData.cpp:31-55), counts the image into the
 // cells its box touches, and the warp reserves its images' ranges of
 // solid-fraction codes with one atomic.
+// Images per block of img_prep (a partial warp): each thread's image record
+// is a long FP64 chain, and FP64 runs at 1/64 of the FP32 rate on this GPU,
+// so the images are spread over as many multiprocessors as possible.
+constexpr int IMG_LANES = 16;
 __global__ void img_prep_kernel(MapParams p) {
+  constexpr unsigned M = IMG_LANES == 32 ? 0xffffffffu : (1u << IMG_LANES) - 1u;
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool mine = i < p.n;
@@ -188,13 +193,13 @@ __global__ void img_prep_kernel(MapParams p) {
   // code ranges: warp prefix of the box volumes, one atomic per warp
   unsigned long long incl = vol;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, o);
+  for (int o = 1; o < IMG_LANES; o <<= 1) {
+    const unsigned long long x = __shfl_up_sync(M, incl, o);
     if (lane >= o) incl += x;
   }
   unsigned long long base = 0;
-  if (lane == 31) base = atomicAdd(&p.pair_total[1], incl);
-  base = __shfl_sync(0xffffffffu, base, 31);
+  if (lane == IMG_LANES - 1) base = atomicAdd(&p.pair_total[1], incl);
+  base = __shfl_sync(M, base, IMG_LANES - 1);
   if (mine) {
     im.sf_off = (long long)(base + incl - vol);
     p.img[i] = im;
@@ -224,7 +229,7 @@ __global__ void img_prep_kernel(MapParams p) {
             (unsigned long long)(cr[5] - cr[2] + 1);
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+  for (int o = IMG_LANES / 2; o > 0; o >>= 1) pairs += __shfl_xor_sync(M, pairs, o);
   if (lane == 0 && pairs) atomicAdd(&p.pair_total[0], pairs);
 }
 
@@ -1125,9 +1130,8 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st, cudaStream_t aux, cu
   const int ncells = p.C[0] * p.C[1] * p.C[2];
   const int tb = 128;
   const unsigned wblocks = (unsigned)(((long long)p.n * 32 + tb - 1) / tb);
-  // one warp per block: a thread's image record is a long FP64 chain, so the
-  // images are spread over as many multiprocessors as possible
-  img_prep_kernel<<<(p.n + 31) / 32, 32, 0, st>>>(p);
+  // IMG_LANES images per block, spread over as many multiprocessors as possible
+  img_prep_kernel<<<(p.n + IMG_LANES - 1) / IMG_LANES, IMG_LANES, 0, st>>>(p);
   const bool two = aux && fork && join;
   cudaStream_t cl = two ? aux : st;
   cudaError_t e;
@@ -1276,14 +1280,15 @@ static __device__ __forceinline__ void two_sum(float a, float b, float& s, float
 // (hi + lo pairs combined with TwoSum, ~48-bit significand) on the FP32 pipe,
 // then the per-warp results summed in FP64.  (FP64 arithmetic runs at 1/64 of
 // the FP32 rate on this GPU.)  Issue- and latency-bound: 64 registers,
-// 128-thread blocks (8 per multiprocessor: 2281 images of the 256^3
-// suspension fill the GPU in finer waves than 256-thread blocks), two nodes'
+// 64-thread blocks (16 per multiprocessor: the 2281 images of the 256^3
+// suspension run in one wave), two nodes'
 // loads in flight per thread, and only the nodes of each row that may lie
 // within rP visited (a sphere holds about half of its box), without the
 // divergence of testing every box node.  The order of the sums is fixed by
 // the image's box alone, so the results are reproducible bit for bit.
 constexpr int RED_U = 2;
-__global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams p) {
+constexpr int RED32_THREADS = 64;  // FP32 reduction block
+__global__ void __launch_bounds__(RED32_THREADS, 16) reduce_f32_kernel(ReduceParams p) {
   const int ip = blockIdx.x;
   const Geom& g = p.g;
   const int tag = p.tag[ip];
@@ -1307,7 +1312,7 @@ __global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams
     // consecutive nodes); a lane finds its node's row by a binary search of
     // the segments' offsets across the warp.
     const float rem0 = bx.rP2f * 1.0001f + 0.01f;
-    for (int r0 = warp * 32; r0 < R; r0 += RED_THREADS) {
+    for (int r0 = warp * 32; r0 < R; r0 += RED32_THREADS) {
       const int r = r0 + lane;
       int xa = bx.qlo[0], len = 0, j = 0, k = 0;
       if (r < R) {
@@ -1451,7 +1456,7 @@ __global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams
     }
   }
   // warps in index order, still in double-float; one FP64 sum per term
-  __shared__ float part_hi[RED_THREADS / 32][12], part_lo[RED_THREADS / 32][12];
+  __shared__ float part_hi[RED32_THREADS / 32][12], part_lo[RED32_THREADS / 32][12];
   if ((lane & 7) == 0) {  // lanes 0, 8, 16, 24 hold terms 0-2, 3-5, 6-8, 9-11
     const int q0 = (up16 ? 6 : 0) + (up8 ? 3 : 0);
 #pragma unroll
@@ -1464,7 +1469,7 @@ __global__ void __launch_bounds__(RED_THREADS, 8) reduce_f32_kernel(ReduceParams
   if (threadIdx.x < 12) {
     const int q = threadIdx.x;
     float sh = 0.0f, sl = 0.0f;
-    for (int w = 0; w < RED_THREADS / 32; ++w) {
+    for (int w = 0; w < RED32_THREADS / 32; ++w) {
       float sv, e;
       two_sum(sh, part_hi[w][q], sv, e);
       sh = sv;
@@ -1493,7 +1498,7 @@ cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st) {
   if (p.nodeF_is_double)
     reduce_f64_kernel<<<p.n, RED_THREADS, 0, st>>>(p);
   else
-    reduce_f32_kernel<<<p.n, RED_THREADS, 0, st>>>(p);
+    reduce_f32_kernel<<<p.n, RED32_THREADS, 0, st>>>(p);
   return cudaGetLastError();
 }
 
