@@ -412,7 +412,7 @@ static __device__ __forceinline__ int corner_count(int dim, float dxf, float dyf
   return -1;
 }
 
-constexpr int SFC_THREADS = 128;  // classification: one block per image
+constexpr int SFC_THREADS = 64;   // classification: one block per image
 constexpr int SFS_THREADS = 128;  // shell counting: persistent warps
 constexpr int SFS_BUF = 352;      // per-warp buffer of crossing rows (>= 32 + 32*10)
 
