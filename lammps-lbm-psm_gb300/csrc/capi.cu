@@ -43,7 +43,7 @@ struct lbmpsm_handle {
   float scale16 = (float)(1 << FP16_SCALE_LOG2);
   // host-pointer steps without staging copies: the device reads and writes
   // pageable host memory through the host's page tables (NVLink-C2C on
-  // Grace), so the gather kernel takes the caller's image arrays and the
+  // Grace), so the image preparation reads the caller's image arrays and the
   // reduction writes the caller's outputs and status_host directly
   bool host_direct = false;
   int status_host = 0;
@@ -106,12 +106,14 @@ struct lbmpsm_handle {
   int sel_box = 0;           // box the reference-layout calls address
   double* out2[3]{};         // lbmpsm_step_device: the caller's F/T/S buffers, written by
                              // the reduction beside the handle's own (null otherwise)
-  // graphs of one device-pointer step for each parity (gather of the caller's
-  // images, map + collide + reduce); the gather and reduce nodes take each
-  // call's pointers
+  const void* src[5]{};      // the caller's tag, x, v, omega, radius arrays, read by the
+                             // map in place and copied into d_tag / d_xvw (null otherwise)
+  // graphs of one device-pointer step for each parity (map reading the
+  // caller's images, collide, reduce); the image-preparation and reduce
+  // nodes take each call's pointers
   cudaGraph_t dgraph[2]{nullptr, nullptr};
   cudaGraphExec_t dexec[2]{nullptr, nullptr};
-  cudaGraphNode_t dgather[2]{nullptr, nullptr}, dreduce[2]{nullptr, nullptr};
+  cudaGraphNode_t dprep[2]{nullptr, nullptr}, dreduce[2]{nullptr, nullptr};
   int dgraph_n = -1;
   int dprev_n = -1;  // image count of the previous device step
   int dsame = 0;     // consecutive device steps with that count
@@ -311,7 +313,7 @@ void drop_device_graphs(lbmpsm_handle* h) {
     if (h->dgraph[k]) cudaGraphDestroy(h->dgraph[k]);
     h->dexec[k] = nullptr;
     h->dgraph[k] = nullptr;
-    h->dgather[k] = h->dreduce[k] = nullptr;
+    h->dprep[k] = h->dreduce[k] = nullptr;
   }
   h->dgraph_n = -1;
 }
@@ -533,6 +535,15 @@ int enqueue_map(lbmpsm_handle* h, int n) {
     m.v = v;
     m.omega = w;
     m.radius = r;
+    if (h->src[0]) {  // read the caller's arrays; leave copies in the handle's buffers
+      m.tag = static_cast<const int*>(h->src[0]);
+      m.x = static_cast<const double*>(h->src[1]);
+      m.v = static_cast<const double*>(h->src[2]);
+      m.omega = static_cast<const double*>(h->src[3]);
+      m.radius = static_cast<const double*>(h->src[4]);
+      m.copy_tag = h->d_tag;
+      m.copy_xvw = h->d_xvw;
+    }
     m.img_box = h->step_boxes ? h->d_img_box : nullptr;
     m.box = h->d_box;
     m.dx = h->dx;
@@ -1108,24 +1119,27 @@ int stage_images(lbmpsm_handle* h, int n, const int* box, const int* tag, const 
 }
 
 // One step from image arrays the device can read (device memory, or host
-// memory when host_direct) into output arrays it can write: the gather
-// kernel copies the images into the handle's buffers, the reduction writes
-// the outputs beside the handle's own.  Asynchronous on the handle's stream.
+// memory when host_direct) into output arrays it can write: the map's image
+// preparation reads the caller's arrays and copies them into the handle's
+// buffers, the reduction writes the outputs beside the handle's own.
+// Asynchronous on the handle's stream.
 int device_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const double* v,
                 const double* omega, const double* radius, double* fh, double* th,
                 double* stresslet) {
   auto enqueue_all = [&]() -> int {
-    CUDA_TRY(h, launch_gather_images(n, tag, x, v, omega, radius, h->d_tag, h->d_xvw, h->stream));
     h->out2[0] = n > 0 ? fh : nullptr;
     h->out2[1] = n > 0 ? th : nullptr;
     h->out2[2] = n > 0 ? stresslet : nullptr;
+    const void* src[5] = {tag, x, v, omega, radius};
+    for (int k = 0; k < 5; ++k) h->src[k] = n > 0 ? src[k] : nullptr;
     const int r = enqueue_step(h, n);
     h->out2[0] = h->out2[1] = h->out2[2] = nullptr;
+    for (int k = 0; k < 5; ++k) h->src[k] = nullptr;
     return r;
   };
   // Replayed as one CUDA graph per parity once the image count has held for
   // two calls (as host steps are); each call writes its own pointers into the
-  // gather and reduce nodes of the executable graph, which affects only the
+  // image-preparation and reduce nodes of the executable graph, which affects only the
   // launches that follow.  Steps that store the macroscopic fields, and steps
   // without images, run eagerly.
   h->dsame = n == h->dprev_n ? h->dsame + 1 : 0;
@@ -1151,7 +1165,7 @@ int device_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
     std::vector<cudaGraphNode_t> nodes(nn);
     if (e == cudaSuccess) e = cudaGraphGetNodes(graph, nodes.data(), &nn);
     cudaGraphNode_t gn = nullptr, rn = nullptr;
-    const void* fg = gather_images_fn();
+    const void* fg = img_prep_fn();
     const void* fr = reduce_fn(h->opt.storage == LBMPSM_STORAGE_FP64 ? 1 : 0);
     for (size_t k = 0; e == cudaSuccess && k < nn; ++k) {
       cudaGraphNodeType ty;
@@ -1167,25 +1181,29 @@ int device_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
       cudaGetLastError();
       cudaGraphDestroy(graph);
       CUDA_TRY(h, e);
-      return fail(h, LBMPSM_ERR_CUDA, "device-step graph: the gather or reduce node was not found");
+      return fail(h, LBMPSM_ERR_CUDA,
+                  "device-step graph: the image-preparation or reduce node was not found");
     }
     h->dgraph[par] = graph;
     h->dexec[par] = ex;
-    h->dgather[par] = gn;
+    h->dprep[par] = gn;
     h->dreduce[par] = rn;
     h->dgraph_n = n;
   }
   {
-    // this call's pointers into the gather and reduce nodes
+    // this call's pointers into the image-preparation and reduce nodes
     cudaKernelNodeParams kp{};
-    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dgather[par], &kp));
-    int* dt = h->d_tag;
-    double* dxvw = h->d_xvw;
-    void* ga[] = {(void*)&n, (void*)&tag, (void*)&x, (void*)&v, (void*)&omega, (void*)&radius,
-                  (void*)&dt, (void*)&dxvw};
+    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dprep[par], &kp));
+    MapParams mp = *static_cast<const MapParams*>(kp.kernelParams[0]);
+    mp.tag = tag;
+    mp.x = x;
+    mp.v = v;
+    mp.omega = omega;
+    mp.radius = radius;
+    void* ga[] = {(void*)&mp};
     kp.kernelParams = ga;
     kp.extra = nullptr;
-    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dgather[par], &kp));
+    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dprep[par], &kp));
     cudaKernelNodeParams rk{};
     CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dreduce[par], &rk));
     ReduceParams rp = *static_cast<const ReduceParams*>(rk.kernelParams[0]);

@@ -324,6 +324,10 @@ struct MapParams {
   double dx;
   double sqrt2half;   // sqrt(2.1)/2 in 2-D, sqrt(3.1)/2 in 3-D (host libm)
   Img* img;
+  // optional copies of the image arrays (tag; x | v | omega | radius), written
+  // by img_prep when it reads a caller's arrays in place
+  int* copy_tag;
+  double* copy_xvw;
   // per image, three int4 for the table update: (lo0 | hi0 << 16, lo1 | hi1 << 16,
   // lo2 | hi2 << 16, tag), (sf_off low, sf_off high, box0 | box1 << 16, has_spin),
   // (uTf[0..2] as bits, 0); an image with an empty box has lo = hi = 0
@@ -476,13 +480,8 @@ cudaError_t launch_map(const MapParams& p, cudaStream_t st, cudaStream_t aux = n
                        cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st);
 // the kernels whose arguments a replayed device-step graph updates per call
-const void* gather_images_fn();
+const void* img_prep_fn();
 const void* reduce_fn(int nodeF_is_double);
-// the image arrays of lbmpsm_step_device into the handle's image buffers
-// (tag[n]; x | v | omega (3n each) | radius (n)) in one launch
-cudaError_t launch_gather_images(int n, const int* tag, const double* x, const double* v,
-                                 const double* omega, const double* radius, int* d_tag,
-                                 double* d_xvw, cudaStream_t st);
 cudaError_t launch_table_export(const Geom& g, const Table& t, int* ids, double* eps,
                                 double* us, cudaStream_t st);
 cudaError_t launch_export_fields(const Geom& g, const Table& t, const double* rho,

@@ -85,6 +85,17 @@ __global__ void img_prep_kernel(MapParams p) {
   if (mine) {
     const Geom& g = p.g;
     im.tag = p.tag[i];
+    if (p.copy_tag) {  // the caller's arrays, kept for later steps with these images
+      const size_t nn = (size_t)p.n;
+      p.copy_tag[i] = im.tag;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        p.copy_xvw[3 * (size_t)i + c] = p.x[3 * (size_t)i + c];
+        p.copy_xvw[3 * nn + 3 * (size_t)i + c] = p.v[3 * (size_t)i + c];
+        p.copy_xvw[6 * nn + 3 * (size_t)i + c] = p.omega[3 * (size_t)i + c];
+      }
+      p.copy_xvw[9 * nn + i] = p.radius[i];
+    }
     im.bidx = p.img_box ? p.img_box[i] : 0;
     im.zoff = im.bidx * g.bz;
     const BoxParams& bp = p.box[im.bidx];
@@ -1502,36 +1513,10 @@ cudaError_t launch_reduce(const ReduceParams& p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// One thread per image: the caller's image arrays into the handle's image
-// block (one launch instead of one copy per array).
-__global__ void gather_images_kernel(int n, const int* __restrict__ tag,
-                                     const double* __restrict__ x, const double* __restrict__ v,
-                                     const double* __restrict__ w, const double* __restrict__ r,
-                                     int* __restrict__ d_tag, double* __restrict__ d_xvw) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const size_t nn = (size_t)n;
-  d_tag[i] = tag[i];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    d_xvw[3 * (size_t)i + c] = x[3 * (size_t)i + c];
-    d_xvw[3 * nn + 3 * (size_t)i + c] = v[3 * (size_t)i + c];
-    d_xvw[6 * nn + 3 * (size_t)i + c] = w[3 * (size_t)i + c];
-  }
-  d_xvw[9 * nn + i] = r[i];
-}
-
-const void* gather_images_fn() { return (const void*)gather_images_kernel; }
+// the kernels whose parameters a replayed device-step graph updates per call
+const void* img_prep_fn() { return (const void*)img_prep_kernel; }
 const void* reduce_fn(int nodeF_is_double) {
   return nodeF_is_double ? (const void*)reduce_f64_kernel : (const void*)reduce_f32_kernel;
-}
-
-cudaError_t launch_gather_images(int n, const int* tag, const double* x, const double* v,
-                                 const double* omega, const double* radius, int* d_tag,
-                                 double* d_xvw, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  gather_images_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, tag, x, v, omega, radius, d_tag, d_xvw);
-  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ exports
