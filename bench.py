@@ -764,8 +764,10 @@ def run_ensemble(args):
                    "classes": per_class,
                    "launch": "one ensemble per edge class; the classes stepped as one group: "
                              "one CUDA graph launch per step for all boxes; the classes' maps and "
-                             "reductions as concurrent branches around ONE collide launch for "
-                             "every box (unless LBMPSM_GROUP_FUSE=0)"},
+                             "reductions as concurrent branches around the collide, which the "
+                             "group's tuner runs as ONE launch for every box or as one launch "
+                             "per class, whichever it timed faster (collide_launches_per_step, "
+                             "group_tuner_ms_per_step)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "kernel": "collide_multi_kernel (one launch for the boxes of every size)"
