@@ -248,6 +248,7 @@ class MovingImages:
         self.radius = torch.as_tensor(np.asarray(g.radius, np.float64), device=dev)
         self.host = (np.asarray(g.tag, np.int32), xs, vs, np.zeros((self.n, 3)),
                      np.asarray(g.radius, np.float64))
+        self.host_out = None  # F/T/S of the host steps, one array reused
         torch.cuda.synchronize(dev)
 
     def step(self, lat, k, bc=True):
@@ -258,10 +259,13 @@ class MovingImages:
             lat.apply_bc()
 
     def host_step(self, lat, k):
-        """The same step through the host-pointer call (pinned copies inside)."""
+        """The same step through the host-pointer call, into one output array
+        that every step reuses (as a host program's force arrays)."""
         t, xs, vs, w, r = self.host
         j = k % self.nsets
-        out = lat.step(t, xs[j], vs[j], w, r)
+        if self.host_out is None:
+            self.host_out = np.empty(12 * len(t))
+        out = lat.step(t, xs[j], vs[j], w, r, out=self.host_out)
         lat.apply_bc()
         return out
 

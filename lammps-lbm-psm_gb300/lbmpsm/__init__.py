@@ -225,14 +225,22 @@ class Lattice:
     def set_bc(self, kind):
         self._check(self.lib.lbmpsm_set_bc(self.h, BC[kind] if isinstance(kind, str) else int(kind)))
 
-    def step(self, tag, x, v, omega, radius):
+    def step(self, tag, x, v, omega, radius, out=None):
+        """One coupling step (lbmpsm_step); returns (fh[n,3], th[n,3], S[n,6]).
+        ``out``: an optional C-contiguous float64 array of at least 12n
+        elements that receives fh | th | S (the returned arrays are views
+        of it), as a host program passes the same arrays every step."""
         tag = np.ascontiguousarray(tag, dtype=np.int32)
         n = len(tag)
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(n, 3)
         v = np.ascontiguousarray(v, dtype=np.float64).reshape(n, 3)
         omega = np.ascontiguousarray(omega, dtype=np.float64).reshape(n, 3)
         radius = np.ascontiguousarray(radius, dtype=np.float64).reshape(n)
-        out = np.empty(12 * n)  # fh | th | S, every element written by the call
+        if out is None:
+            out = np.empty(12 * n)  # fh | th | S, every element written by the call
+        elif (out.dtype != np.float64 or not out.flags.c_contiguous or out.size < 12 * n):
+            raise ValueError("out must be a C-contiguous float64 array of at least 12n elements")
+        out = out.reshape(-1)
         a = out.ctypes.data
         self._check(self.lib.step_by_address(
             self.h, n, tag.ctypes.data, x.ctypes.data, v.ctypes.data, omega.ctypes.data,

@@ -257,9 +257,11 @@ def test_host_steps_in_place_equal_staged_steps(storage, monkeypatch):
     b = _lat(case, storage)
     monkeypatch.delenv("LBMPSM_HOST_STAGING")
     assert not b.host_direct
+    buf = np.empty(12 * 64)  # one output array for every step of a (out=)
     for _ in range(9):
         g = cases.images(case, tag, x, v, w, r, cases.product_make_ghosts)
-        fa = a.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"]); a.apply_bc()
+        assert 12 * len(g["tag"]) <= buf.size
+        fa = a.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"], out=buf); a.apply_bc()
         fb = b.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"]); b.apply_bc()
         for p, q in zip(fa, fb):
             assert np.array_equal(p, q)
@@ -271,3 +273,5 @@ def test_host_steps_in_place_equal_staged_steps(storage, monkeypatch):
     bad[0, 0] = np.nan
     with pytest.raises(lbmpsm.LbmPsmError):
         a.step(g["tag"], bad, g["v"], g["omega"], g["radius"])
+    with pytest.raises(ValueError):
+        a.step(g["tag"], g["x"], g["v"], g["omega"], g["radius"], out=np.empty(3))
