@@ -245,7 +245,8 @@ class Lattice:
         self._check(self.lib.step_by_address(
             self.h, n, tag.ctypes.data, x.ctypes.data, v.ctypes.data, omega.ctypes.data,
             radius.ctypes.data, a, a + 24 * n, a + 48 * n))
-        return out[:3 * n].reshape(n, 3), out[3 * n:6 * n].reshape(n, 3), out[6 * n:].reshape(n, 6)
+        return (out[:3 * n].reshape(n, 3), out[3 * n:6 * n].reshape(n, 3),
+                out[6 * n:12 * n].reshape(n, 6))
 
     @staticmethod
     def _images(tag, x, v, omega, radius):
