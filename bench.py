@@ -110,6 +110,13 @@ MOVE_AMP = 0.1      # lattice units: each sphere walks a closed loop of this rad
 MOVE_SEED = 20261205
 
 
+def suspension_workload(edge, nspheres):
+    """The suspension workload's description, the same for both arms."""
+    return (f"sheared suspension: D3Q19 {edge}^3, y Zou-He shear walls +-0.01, tau 0.65, "
+            f"{nspheres} spheres D=12 (seeded RSA, phi~0.108 at 256^3) moving on seeded closed "
+            f"loops (new positions every step)")
+
+
 def moving_image_sets(g, nloc, nsets=MOVE_SETS, amp=MOVE_AMP, seed=MOVE_SEED):
     """Positions and velocities of the images for nsets consecutive steps: every
     sphere moves on its own seeded closed loop (an ellipse of radius `amp`
@@ -407,9 +414,8 @@ def run_ours(args, rank=0, world=1):
         "dtype": "f32",  # FP32 collision arithmetic (FP32 or FP16 storage)
         "data": "synthetic",
         "config": {
-            "workload": f"sheared suspension: D3Q19 {edge}^3, y Zou-He shear walls +-0.01, tau 0.65, "
-                        f"{nloc} spheres D=12 (seeded RSA) moving on seeded closed loops (new "
-                        f"positions every step), {args.storage.upper()} storage, FP64 F/T/S",
+            "workload": suspension_workload(edge, nloc) + f", {args.storage.upper()} storage, "
+                                                          "FP64 F/T/S",
             "nodes": nodes, "particles": nloc, "images": n, "storage": args.storage,
             "motion": f"every sphere on its own closed loop of radius {MOVE_AMP} lattice units, "
                       f"period {MOVE_SETS} steps (top speed ~0.02 lattice units per step); "
@@ -554,25 +560,29 @@ def cpu_baseline(steps, threads=None, single_core=False):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liblbmpsm_oracle.so"], check=True)
     threads = threads or os.cpu_count()
     g, nloc = images()
+    xs, vs = moving_image_sets(g, nloc)  # the GPU arm's moving images, step by step
     prm = workload_params()
     prm["bc_type"] = 1
     sim = pyoracle.Sim("restatement", **prm)
     sim.set_threads(threads)
-    sim.step(g.tag, g.x, g.v, g.omega, g.radius, bc=True)  # warm-up (first touch)
+    sim.step(g.tag, xs[0], vs[0], g.omega, g.radius, bc=True)  # warm-up (first touch)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        sim.step(g.tag, g.x, g.v, g.omega, g.radius, bc=True)
+    for k in range(1, steps + 1):
+        j = k % len(xs)
+        sim.step(g.tag, xs[j], vs[j], g.omega, g.radius, bc=True)
     dt = time.perf_counter() - t0
     nodes = EDGE ** 3
     out = {"value": round(nodes * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": threads,
            "kind": "port",
-           "sample": f"{steps} full coupling steps of the same 256^3 / 2000-sphere workload "
-                     f"(after 1 warm-up step), FP64, OpenMP over {threads} threads",
+           "sample": f"{steps} full coupling steps of the same 256^3 / 2000-sphere workload, "
+                     f"spheres moving on the same loops (after 1 warm-up step), FP64, OpenMP "
+                     f"over {threads} threads",
            "seconds": round(dt, 2)}
     if single_core:
         sim.set_threads(1)
         t0 = time.perf_counter()
-        sim.step(g.tag, g.x, g.v, g.omega, g.radius, bc=True)
+        j = (steps + 1) % len(xs)
+        sim.step(g.tag, xs[j], vs[j], g.omega, g.radius, bc=True)
         d1 = time.perf_counter() - t0
         out["single_core"] = {"value": round(nodes / d1 / 1e6, 3), "unit": "MLUPS", "cores": 1,
                               "sample": "1 full coupling step, one thread", "seconds": round(d1, 2)}
@@ -594,9 +604,12 @@ def run_reference(args, rank, world):
         "ms_per_step": round(cb["seconds"] / steps * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": "sheared suspension: D3Q19 256^3, y Zou-He shear walls +-0.01, "
-                               "tau 0.65, 2000 spheres D=12 (seeded RSA, phi~0.108)",
-                   "nodes": nodes, "parallelism": f"{cb['cores']} host threads"},
+        "config": {"workload": suspension_workload(EDGE, NSPHERES) + ", FP64 (the reference's "
+                                                                      "arithmetic)",
+                   "nodes": nodes, "particles": NSPHERES,
+                   "motion": f"the same closed loops as the GPU arm (radius {MOVE_AMP}, period "
+                             f"{MOVE_SETS} steps)",
+                   "parallelism": f"{cb['cores']} host threads"},
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
