@@ -114,6 +114,10 @@ struct lbmpsm_handle {
   cudaGraph_t dgraph[2]{nullptr, nullptr};
   cudaGraphExec_t dexec[2]{nullptr, nullptr};
   cudaGraphNode_t dprep[2]{nullptr, nullptr}, dreduce[2]{nullptr, nullptr};
+  // the parameters those two nodes hold in the executable graph
+  cudaKernelNodeParams dprep_kp[2]{}, dreduce_kp[2]{};
+  MapParams dprep_p[2]{};
+  ReduceParams dreduce_p[2]{};
   int dgraph_n = -1;
   int dprev_n = -1;  // image count of the previous device step
   int dsame = 0;     // consecutive device steps with that count
@@ -1184,6 +1188,23 @@ int device_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
       return fail(h, LBMPSM_ERR_CUDA,
                   "device-step graph: the image-preparation or reduce node was not found");
     }
+    // the captured parameters (this call's pointers already)
+    cudaKernelNodeParams kp{}, rk{};
+    e = cudaGraphKernelNodeGetParams(gn, &kp);
+    if (e == cudaSuccess) e = cudaGraphKernelNodeGetParams(rn, &rk);
+    if (e != cudaSuccess) {
+      cudaGraphExecDestroy(ex);
+      cudaGraphDestroy(graph);
+      CUDA_TRY(h, e);
+    }
+    h->dprep_p[par] = *static_cast<const MapParams*>(kp.kernelParams[0]);
+    h->dreduce_p[par] = *static_cast<const ReduceParams*>(rk.kernelParams[0]);
+    kp.kernelParams = nullptr;
+    kp.extra = nullptr;
+    rk.kernelParams = nullptr;
+    rk.extra = nullptr;
+    h->dprep_kp[par] = kp;
+    h->dreduce_kp[par] = rk;
     h->dgraph[par] = graph;
     h->dexec[par] = ex;
     h->dprep[par] = gn;
@@ -1191,29 +1212,30 @@ int device_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
     h->dgraph_n = n;
   }
   {
-    // this call's pointers into the image-preparation and reduce nodes
-    cudaKernelNodeParams kp{};
-    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dprep[par], &kp));
-    MapParams mp = *static_cast<const MapParams*>(kp.kernelParams[0]);
-    mp.tag = tag;
-    mp.x = x;
-    mp.v = v;
-    mp.omega = omega;
-    mp.radius = radius;
-    void* ga[] = {(void*)&mp};
-    kp.kernelParams = ga;
-    kp.extra = nullptr;
-    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dprep[par], &kp));
-    cudaKernelNodeParams rk{};
-    CUDA_TRY(h, cudaGraphKernelNodeGetParams(h->dreduce[par], &rk));
-    ReduceParams rp = *static_cast<const ReduceParams*>(rk.kernelParams[0]);
-    rp.fh2 = fh;
-    rp.th2 = th;
-    rp.S2 = stresslet;
-    void* ra[] = {(void*)&rp};
-    rk.kernelParams = ra;
-    rk.extra = nullptr;
-    CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dreduce[par], &rk));
+    // this call's pointers into the image-preparation and reduce nodes, where
+    // they differ from the ones the executable graph holds
+    MapParams& mp = h->dprep_p[par];
+    if (mp.tag != tag || mp.x != x || mp.v != v || mp.omega != omega || mp.radius != radius) {
+      mp.tag = tag;
+      mp.x = x;
+      mp.v = v;
+      mp.omega = omega;
+      mp.radius = radius;
+      void* ga[] = {(void*)&mp};
+      cudaKernelNodeParams kp = h->dprep_kp[par];
+      kp.kernelParams = ga;
+      CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dprep[par], &kp));
+    }
+    ReduceParams& rp = h->dreduce_p[par];
+    if (rp.fh2 != fh || rp.th2 != th || rp.S2 != stresslet) {
+      rp.fh2 = fh;
+      rp.th2 = th;
+      rp.S2 = stresslet;
+      void* ra[] = {(void*)&rp};
+      cudaKernelNodeParams rk = h->dreduce_kp[par];
+      rk.kernelParams = ra;
+      CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->dexec[par], h->dreduce[par], &rk));
+    }
   }
   CUDA_TRY(h, cudaGraphLaunch(h->dexec[par], h->stream));
   h->t += 1;
