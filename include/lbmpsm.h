@@ -161,9 +161,11 @@ int lbmpsm_step(lbmpsm_handle* h, int n, const int* tag, const double* x, const 
                 const double* omega, const double* radius, double* fh, double* th,
                 double* stresslet);
 /* Same, with all arrays in device memory; asynchronous on the handle's
- * stream.  Requires opts.max_radius >= every radius.  The outputs (each may
- * be NULL) are written by the step's own reduction; the handle keeps a copy
- * as well (lbmpsm_read_forces). */
+ * stream.  Requires opts.max_radius >= every radius.  The step reads the
+ * image arrays in place (and keeps copies for lbmpsm_run_fixed); the outputs
+ * (each may be NULL) are written by the step's own reduction, and the handle
+ * keeps a copy as well (lbmpsm_read_forces).  The arrays may differ from
+ * call to call. */
 int lbmpsm_step_device(lbmpsm_handle* h, int n, const int* tag, const double* x,
                        const double* v, const double* omega, const double* radius, double* fh,
                        double* th, double* stresslet);
@@ -215,7 +217,7 @@ int lbmpsm_synchronize(lbmpsm_handle* h);
 void* lbmpsm_stream(lbmpsm_handle* h);
 /* 1 when lbmpsm_step works on the caller's host arrays in place: the device
  * reads pageable host memory through the host's page tables (NVLink-C2C on
- * Grace), so the step's gather kernel reads the images and its reduction
+ * Grace), so the step's image preparation reads the images and its reduction
  * writes fh, th and stresslet with no staging copies; 0 when the images are
  * staged through pinned memory and copied (devices without that access, or
  * the environment variable LBMPSM_HOST_STAGING=1 at lbmpsm_create); -1 for
